@@ -1,0 +1,416 @@
+"""Benchmark: 20-qubit VQC value+grad circuits/s on one GB300.
+
+Workload (one "step"): a batch of 1024 independent parameter vectors of the
+20-qubit ansatz with 10 layers of RX, RY, RZ on every qubit followed by a CNOT
+ladder (600 parameters, 790 gates), outputs <Z_i> for every qubit and
+<Z_0 Z_1> (21 expectation values), evaluated forward and differentiated with
+respect to all 600 parameters (adjoint method), complex64 state.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``value`` is circuits/s with parameters
+resident in HBM; ``e2e`` is the same through the public API with the
+parameters in pinned host memory and the gradients/outputs copied back every
+step.  ``roofline`` is computed from CUDA events around every kernel launch of
+the timed region (on the launch stream).  ``--impl reference`` times the
+reference algorithm (TeD-Q's per-gate tensordot state-vector loop with torch
+autograd, restated in ``oracle/``) on the host CPU cores.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "ted-q_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "20q VQC value+grad circuits/s"
+UNIT = "circuits/s"
+
+
+def vqc_spec(n, layers, seed=0):
+    """Seeded synthetic config-2 circuit (angles drawn uniform[0, 2pi))."""
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers):
+        for q in range(n):
+            for name in ("RX", "RY", "RZ"):
+                gates.append({"name": name, "qubits": [q], "params": [float(rng.uniform(0, 2 * np.pi))],
+                              "trainable": [0]})
+        for q in range(n - 1):
+            gates.append({"name": "CNOT", "qubits": [q, q + 1], "params": [], "trainable": []})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
+    meas.append({"kind": "expval", "list": True,
+                 "obs": [{"name": "PauliZ", "qubits": [0]}, {"name": "PauliZ", "qubits": [1]}]})
+    return {"n": n, "gates": gates, "meas": meas, "init_state": None}
+
+
+def workload_config(a):
+    return {"workload": f"vqc{a.qubits}q_{a.layers}layers_batch{a.batch}",
+            "n_qubits": a.qubits, "layers": a.layers, "batch_per_gpu": a.batch,
+            "params_per_circuit": 3 * a.qubits * a.layers, "gates": (4 * a.qubits - 1) * a.layers,
+            "outputs": f"<Z_i> i<{a.qubits} and <Z_0 Z_1>", "gradient": "adjoint, all parameters",
+            "l2": "inputs larger than L2 (state %d MiB per circuit x batch)" % ((8 << a.qubits) >> 20)}
+
+
+# ---------------------------------------------------------------- helpers
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, dev):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU reference
+
+def cpu_reference(spec, n_circuits, seed=1):
+    """Reference algorithm on the host: per-gate tensordot loop with torch
+    autograd (back_prop), complex64, all host threads.  Returns (circuits/s, secs)."""
+    import oracle
+    P = sum(len(g["trainable"]) for g in spec["gates"])
+    gen = torch.Generator().manual_seed(seed)
+    dy = np.ones(len(spec["meas"]))
+    t0 = time.perf_counter()
+    for _ in range(n_circuits):
+        p = torch.rand(P, generator=gen) * 2 * np.pi
+        oracle.value_and_grad(spec, p, dy, torch.complex64)
+    dt = time.perf_counter() - t0
+    return n_circuits / dt, dt
+
+
+def cpu_sample_size(spec, budget_s):
+    rate, dt = cpu_reference(spec, 1)
+    return max(1, int(budget_s / max(dt, 1e-3))), rate, dt
+
+
+def run_reference_arm(a):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    spec = vqc_spec(a.qubits, a.layers)
+    threads = torch.get_num_threads()
+    k, _, _ = cpu_sample_size(spec, a.cpu_budget / max(1, a.steps))
+    k = min(k, 4)
+    for _ in range(a.warmup):
+        cpu_reference(spec, 1)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        cpu_reference(spec, k)
+    dt = time.perf_counter() - t0
+    rate = a.steps * k / dt
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * dt / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": workload_config(a),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{k} circuit(s) of the workload per step, value+grad by back_prop"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- plain per-circuit GPU path
+
+def plain_gpu_rate(spec, dev, n_circuits=2):
+    """The reference's algorithm run per circuit on the GPU with torch ops: one
+    tensordot + permute per gate (pytorch_backend.py:358-380), measurements by
+    tensordot, gradient by torch autograd.  Returns circuits/s (value+grad)."""
+    n = spec["n"]
+    gen = torch.Generator().manual_seed(3)
+    P = sum(len(g["trainable"]) for g in spec["gates"])
+
+    def one(p):
+        k = 0
+        state = torch.zeros([2] * n, dtype=torch.complex64, device=dev)
+        state.view(-1)[0] = 1
+        cnot = torch.tensor([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=torch.complex64,
+                            device=dev).reshape(2, 2, 2, 2)
+        for g in spec["gates"]:
+            q = g["qubits"]
+            if g["name"] == "CNOT":
+                G = cnot
+            else:
+                th = p[k:k + 1]
+                k += 1
+                c, s = torch.cos(th / 2), torch.sin(th / 2)
+                z = torch.zeros_like(c)
+                if g["name"] == "RX":
+                    G = torch.cat([c + 0j, -1j * s, -1j * s, c + 0j]).reshape(2, 2)
+                elif g["name"] == "RY":
+                    G = torch.cat([c, -s, s, c]).to(torch.complex64).reshape(2, 2)
+                else:
+                    e = torch.exp(-0.5j * th)
+                    G = torch.cat([e, z + 0j, z + 0j, e.conj()]).reshape(2, 2)
+            kq = len(q)
+            new = torch.tensordot(G, state, (list(range(kq, 2 * kq)), q))
+            rest = [x for x in range(n) if x not in q]
+            order = list(q) + rest
+            state = new.permute([order.index(i) for i in range(n)])
+        outs = []
+        Z = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex64, device=dev)
+        axes = list(range(n))
+        for obs in ([[q] for q in range(n)] + [[0, 1]]):
+            ms = state
+            for q in obs:
+                ms = torch.tensordot(Z, ms, ([1], [q])).permute(list(range(1, q + 1)) + [0] + list(range(q + 1, n)))
+            outs.append(torch.tensordot(torch.conj(state), ms, (axes, axes)).real)
+        return torch.stack(outs)
+
+    p = (torch.rand(P, generator=gen) * 2 * np.pi).to(dev).requires_grad_(True)
+    one(p).sum().backward()  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n_circuits):
+        p = (torch.rand(P, generator=gen) * 2 * np.pi).to(dev).requires_grad_(True)
+        one(p).sum().backward()
+    torch.cuda.synchronize()
+    return n_circuits / (time.perf_counter() - t0)
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_ours(a):
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    import tedq_gb300 as qai
+    from tedq_gb300 import _lib
+
+    spec = vqc_spec(a.qubits, a.layers)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain)
+    info = cc.program_info
+    P = cc.num_params
+    B = a.batch
+    gen = torch.Generator().manual_seed(1000 + rank)
+    params_host = (torch.rand(a.steps + a.warmup, B, P, generator=gen) * 2 * np.pi)
+    params_dev = params_host.to(dev)
+    L = _lib.lib()
+    h = cc._prog.handle
+    stream = torch.cuda.current_stream(dev)
+
+    def step_dev(i):
+        p = params_dev[i].requires_grad_(True)
+        out = cc.execute_batch(p)
+        out.sum().backward()
+        return out, p.grad
+
+    for i in range(a.warmup):
+        step_dev(i)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    L.tedq_profile_enable(h, 1)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(a.steps):
+        step_dev(a.warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    L.tedq_profile_enable(h, 0)
+    prof = _lib.Profile()
+    _lib.check(L.tedq_profile_read(h, prof), "tedq_profile_read")
+    clk = clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
+    value = world * B * a.steps / (ms / 1000.0)
+
+    # e2e through the public API with host buffers
+    ph = params_host.pin_memory()
+    for i in range(min(2, a.warmup)):
+        p = ph[i].clone().requires_grad_(True)
+        out = cc.execute_batch(p)
+        out.sum().backward()
+        out.cpu()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for i in range(a.steps):
+        p = ph[a.warmup + i].detach().requires_grad_(True)   # pinned host parameters
+        out = cc.execute_batch(p)                             # H2D inside
+        out.sum().backward()                                  # gradients land on the host tensor (D2H)
+        res = out.detach().cpu()                              # outputs D2H
+        _ = p.grad.numpy()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms_e2e = max_over_ranks(max(f0.elapsed_time(f1), 1000 * wall), world, dev)
+    e2e = world * B * a.steps / (ms_e2e / 1000.0)
+
+    if rank != 0:
+        return 0
+
+    hbm_peak, peak_kind = read_peaks()
+    fam = "bwd" if prof.bwd_ms >= prof.fwd_ms else "fwd"
+    launches = getattr(prof, f"{fam}_launches")
+    amp_passes = getattr(prof, f"{fam}_amp_passes")
+    kms = getattr(prof, f"{fam}_ms")
+    bytes_per_amp = 32 if fam == "bwd" else 16
+    per_launch_bytes = bytes_per_amp * amp_passes / max(1, launches)
+    achieved = per_launch_bytes / (kms / max(1, launches) / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "sv_pass_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                t = json.load(f)
+            traffic = t.get(f"{fam}_pass_bytes_per_amp_per_circuit")
+            if traffic is not None:
+                traffic = traffic * amp_passes / max(1, launches)
+        except Exception:
+            traffic = None
+    gpu_launches = prof.fwd_launches + prof.bwd_launches + prof.meas_launches + prof.lam_launches
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64", "data": "synthetic", "config": workload_config(a),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4,
+                    "d2h_bytes_per_step": B * P * 4 + B * info["n_real_outputs"] * 4},
+            "gpu_launches": int(gpu_launches),
+            "roofline": {"bound": "hbm", "kernel": f"{fam}_pass_kernel", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
+                         "avg_launch_ms": kms / max(1, launches)},
+            "kernels_ms_per_step": {"fwd_pass": prof.fwd_ms / a.steps, "bwd_pass": prof.bwd_ms / a.steps,
+                                    "measure": prof.meas_ms / a.steps, "lambda_etc": prof.lam_ms / a.steps},
+            "schedule": {k: info[k] for k in ("n_fwd_passes", "n_bwd_passes", "n_fwd_phases", "n_bwd_phases",
+                                              "n_fused_gates", "n_elem_gates")},
+            "clocks": clk}
+    if not a.no_plain:
+        try:
+            line["plain_gpu_per_circuit"] = {"value": plain_gpu_rate(spec, dev), "unit": UNIT,
+                                             "what": "reference algorithm per circuit with torch ops on the GPU"}
+            line["plain_gpu_per_circuit"]["speedup_of_value"] = value / line["plain_gpu_per_circuit"]["value"]
+        except Exception as e:  # pragma: no cover
+            line["plain_gpu_per_circuit"] = {"error": str(e)[:200]}
+    if not a.no_cpu:
+        spec_cpu = vqc_spec(a.qubits, a.layers)
+        k, _, _ = cpu_sample_size(spec_cpu, a.cpu_budget)
+        k = min(k, 8)
+        rate, dt = cpu_reference(spec_cpu, k)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": f"{k} circuit(s) of the workload, value+grad by back_prop, {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=20)
+    ap.add_argument("--layers", type=int, default=10)
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    a = ap.parse_args()
+    if a.impl == "reference":
+        return run_reference_arm(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,206 @@
+/*
+ * tedq_gb300.h -- C ABI of the GB300 (sm_103a) execution backend for TeD-Q's
+ * compiled-circuit state-vector path.
+ *
+ * Boundary.  The reference executes a recorded circuit in
+ * ``PyTorchBackend.__call__`` / ``execute`` (tedq/backends/pytorch_backend.py
+ * :124-165, :228-391) after ``CompiledCircuit.__init__`` turned the circuit
+ * into per-gate tensordot axes and permutations
+ * (tedq/backends/compiled_circuit.py:48-202).  This library replaces that
+ * pair: ``tedq_program_create`` is the compile step, ``tedq_run`` the
+ * state-vector forward with its measurement reductions
+ * (pytorch_backend.py:358-498) and ``tedq_run_adjoint`` the backward that the
+ * reference obtains from torch autograd (``back_prop``, :142-144) or from
+ * parameter-shift re-execution (``TorchExecute``, :1191-1223).
+ *
+ * Conventions (identical to the reference):
+ *   - qubit q is bit (n-1-q) of the flat amplitude index (qubit 0 is the most
+ *     significant axis of the ``[2]*n`` state, pytorch_backend.py:513-522);
+ *   - a k-qubit gate matrix is indexed with qubits[0] as its most significant
+ *     bit (pytorch_backend.py:741-750);
+ *   - parameters are bound positionally: slot s of a circuit is the s-th
+ *     trainable parameter walking the gates in order
+ *     (compiled_circuit.py:492-547).  Slots are given per gate in
+ *     ``tedq_gate_t.param_slot``.
+ *
+ * All device buffers are owned by the caller and passed as raw device
+ * pointers; streams are ``cudaStream_t`` values passed as ``void*``.  No C++
+ * exception crosses this boundary: every entry point returns a
+ * ``tedq_status`` and ``tedq_last_error`` returns the message of the last
+ * failure on the calling thread.
+ */
+#ifndef TEDQ_GB300_H
+#define TEDQ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TEDQ_ABI_VERSION 1
+
+typedef enum tedq_status {
+  TEDQ_OK = 0,
+  TEDQ_ERR_ARG = 1,         /* bad argument: sizes, qubit indices, null pointers   */
+  TEDQ_ERR_OOM = 2,         /* host allocation failed or a size exceeds a limit    */
+  TEDQ_ERR_CUDA = 3,        /* a CUDA runtime call failed                          */
+  TEDQ_ERR_TIMEOUT = 4,     /* a bounded wait expired                              */
+  TEDQ_ERR_UNSUPPORTED = 5, /* gate/observable form this backend does not execute  */
+  TEDQ_ERR_STATE = 6        /* call made in the wrong state (e.g. stopped server)  */
+} tedq_status;
+
+/* Gate opcodes: the reference's gate set (tedq/QInterpreter/operators/qubit.py
+ * ``ops``, :1803-1834).  TEDQ_OP_MATRIX carries a fixed matrix (the
+ * reference's path for gates without trainable parameters,
+ * compiled_circuit.py:432-435, and for ``.inv`` gates). */
+enum {
+  TEDQ_OP_I = 0, TEDQ_OP_H = 1, TEDQ_OP_X = 2, TEDQ_OP_Y = 3, TEDQ_OP_Z = 4,
+  TEDQ_OP_S = 5, TEDQ_OP_T = 6, TEDQ_OP_SX = 7,
+  TEDQ_OP_CNOT = 8, TEDQ_OP_CZ = 9, TEDQ_OP_CY = 10, TEDQ_OP_SWAP = 11,
+  TEDQ_OP_CSWAP = 12, TEDQ_OP_TOFFOLI = 13,
+  TEDQ_OP_RX = 14, TEDQ_OP_RY = 15, TEDQ_OP_RZ = 16, TEDQ_OP_ROT = 17,
+  TEDQ_OP_PHASESHIFT = 18, TEDQ_OP_CPHASE = 19,
+  TEDQ_OP_CRX = 20, TEDQ_OP_CRY = 21, TEDQ_OP_CRZ = 22,
+  TEDQ_OP_MATRIX = 23
+};
+
+/* One gate of a recorded circuit (one ``GateBase`` instance,
+ * tedq/QInterpreter/operators/ops_abc.py:227-340). */
+typedef struct tedq_gate {
+  int32_t op;             /* TEDQ_OP_*                                             */
+  int32_t n_qubits;       /* 1..3                                                  */
+  int32_t qubits[3];      /* qubits[0] is the control / most significant factor     */
+  int32_t param_slot[3];  /* parameter slot per gate parameter, -1 = fixed          */
+  double fixed[3];        /* value of each parameter whose slot is -1               */
+  const double* matrix;   /* TEDQ_OP_MATRIX: 2^k x 2^k row-major (re, im) pairs     */
+} tedq_gate_t;
+
+/* Observable factor codes for expectation values
+ * (measurement.py ``expval``, :106-155). */
+enum { TEDQ_OBS_I = 0, TEDQ_OBS_X = 1, TEDQ_OBS_Y = 2, TEDQ_OBS_Z = 3, TEDQ_OBS_H = 4,
+       TEDQ_OBS_MATRIX = 5 };
+
+typedef struct tedq_obs_factor {
+  int32_t obs;            /* TEDQ_OBS_*                                            */
+  int32_t n_qubits;       /* 1..3 (only TEDQ_OBS_MATRIX may exceed 1)              */
+  int32_t qubits[3];
+  const double* matrix;   /* TEDQ_OBS_MATRIX: 2^k x 2^k (re, im) pairs              */
+} tedq_obs_factor_t;
+
+/* Measurement kinds (measurement.py ``MeasurementReturnTypes``, :240-266). */
+enum { TEDQ_MEAS_EXPVAL = 0, TEDQ_MEAS_PROBS = 1, TEDQ_MEAS_STATE = 2 };
+
+typedef struct tedq_meas {
+  int32_t kind;                      /* TEDQ_MEAS_*                                 */
+  int32_t n_factors;                 /* EXPVAL: factors of the tensor product,      */
+  const tedq_obs_factor_t* factors;  /*   applied in list order (pytorch_backend.py:402-424) */
+  int32_t n_qubits;                  /* PROBS: measured qubits, 0 = all             */
+  const int32_t* qubits;
+} tedq_meas_t;
+
+enum { TEDQ_PREC_C64 = 0, TEDQ_PREC_C128 = 1 };
+
+typedef struct tedq_options {
+  int32_t precision;   /* TEDQ_PREC_C64 (complex64 state, float32 params/outputs)
+                          or TEDQ_PREC_C128 (complex128 state, float64)            */
+  int32_t fuse;        /* 1: fused multi-gate passes; 0: one pass per gate (plain) */
+  int32_t tile_qubits; /* 0 = default tile size (2^13 amplitudes for c64)          */
+  int32_t reserved[5];
+} tedq_options_t;
+
+typedef struct tedq_program tedq_program_t;
+
+typedef struct tedq_program_info {
+  int32_t n_qubits;          /* logical qubits                                     */
+  int32_t state_qubits;      /* qubits of the device state (>= n_qubits; small
+                                circuits are padded with idle low-order qubits)    */
+  int32_t n_params;          /* parameter slots per circuit                        */
+  int32_t n_real_outputs;    /* floats per circuit written to out_real             */
+  int32_t n_terms;           /* distinct Pauli strings measured                    */
+  int32_t n_fwd_passes;      /* HBM passes of the forward schedule                 */
+  int32_t n_bwd_passes;      /* HBM passes of the adjoint schedule                 */
+  int32_t n_fwd_phases;      /* register phases of the forward schedule            */
+  int32_t n_bwd_phases;
+  int32_t n_fused_gates;     /* gates after fusion (forward)                       */
+  int32_t n_elem_gates;      /* elementary gates (adjoint)                         */
+  int32_t precision;
+  int64_t workspace_per_circuit; /* bytes of workspace per circuit of a batch      */
+  int64_t reserved[4];
+} tedq_program_info_t;
+
+/* ---- library ------------------------------------------------------------ */
+int32_t tedq_abi_version(void);
+/* Message of the last failed call on this thread; returns its length. */
+int32_t tedq_last_error(char* buf, size_t len);
+
+/* ---- program: compile a recorded circuit --------------------------------
+ * Replaces CompiledCircuit.__init__ (compiled_circuit.py:48-202): classifies
+ * gates (diagonal / permutation / controlled / dense), fuses runs of
+ * one-qubit gates, schedules the gate list into HBM passes over 2^m-amplitude
+ * tiles and register phases inside each tile, and decomposes observables into
+ * Pauli strings.  ``opts`` may be NULL (defaults). */
+int32_t tedq_program_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n_qubits,
+                            const tedq_meas_t* meas, int32_t n_meas,
+                            const tedq_options_t* opts, tedq_program_t** out);
+int32_t tedq_program_destroy(tedq_program_t* prog);
+int32_t tedq_program_info(const tedq_program_t* prog, tedq_program_info_t* info);
+/* Device workspace (bytes) that tedq_run / tedq_run_adjoint need for a batch. */
+int64_t tedq_program_workspace_bytes(const tedq_program_t* prog, int64_t batch);
+/* Schedule export for inspection: writes a JSON description of the passes
+ * and phases (forward when ``adjoint`` == 0) into ``buf``; returns the
+ * length needed including the terminating zero. */
+int64_t tedq_program_describe(const tedq_program_t* prog, int32_t adjoint, char* buf, int64_t len);
+
+/* ---- forward: PyTorchBackend.execute, state-vector branch ---------------
+ * params    [batch][n_params]          float (c64) / double (c128), device
+ * psi       [batch][2^state_qubits]    complex, device; receives final states
+ * out_real  [batch][n_real_outputs]    float / double, device; expvals then
+ *                                      probs, in measurement order (may be NULL
+ *                                      when the program has no real outputs)
+ * init      [2^n_qubits] complex initial state shared by the batch, or NULL
+ *           for |0...0> (pytorch_backend.py:500-522)
+ * workspace >= tedq_program_workspace_bytes(batch) bytes, device, 256-byte
+ *           aligned (Pauli-term, probability and gradient accumulators) */
+int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* psi,
+                 void* out_real, const void* init, void* workspace, size_t workspace_bytes,
+                 void* stream);
+
+/* ---- adjoint backward ----------------------------------------------------
+ * Vector-Jacobian product of tedq_run: grad[b][s] = d/dparam[b][s] of
+ *   sum_k dy_real[b][k] * out_real[b][k] + Re sum_x conj(dy_state[b][x]) psi[b][x]
+ * psi       final states from tedq_run; overwritten (uncomputed to the
+ *           initial state)
+ * lambda_   [batch][2^state_qubits] complex device scratch
+ * dy_real   [batch][n_real_outputs] or NULL; dy_state [batch][2^state_qubits]
+ *           complex or NULL
+ * grad      [batch][n_params] float / double, device, written */
+int32_t tedq_run_adjoint(tedq_program_t* prog, const void* params, int64_t batch,
+                         const void* dy_real, const void* dy_state, void* psi, void* lambda_,
+                         void* grad, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- profiling -----------------------------------------------------------
+ * When enabled, tedq_run / tedq_run_adjoint record a CUDA event pair on the
+ * launch stream around every kernel launch of the program; tedq_profile_read
+ * synchronises those events, returns the accumulated device time per kernel
+ * family and clears the record.  No reference counterpart (the reference has
+ * no tracing, only ad-hoc wall clocks in its examples). */
+typedef struct tedq_profile {
+  int64_t fwd_launches;   double fwd_ms;    /* forward pass kernels              */
+  int64_t bwd_launches;   double bwd_ms;    /* adjoint pass kernels              */
+  int64_t meas_launches;  double meas_ms;   /* expval / probs / finalize kernels */
+  int64_t lam_launches;   double lam_ms;    /* lambda init, weights, grad finalize */
+  int64_t fwd_amp_passes; /* sum over forward launches of batch * 2^state_qubits */
+  int64_t bwd_amp_passes; /* same for adjoint launches                           */
+  int64_t reserved[4];
+} tedq_profile_t;
+
+int32_t tedq_profile_enable(tedq_program_t* prog, int32_t on);
+int32_t tedq_profile_read(tedq_program_t* prog, tedq_profile_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TEDQ_GB300_H */

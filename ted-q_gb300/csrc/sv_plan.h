@@ -1,0 +1,138 @@
+// sv_plan.h -- the compiled state-vector schedule shared by the host
+// scheduler (sv_program.cpp) and the CUDA kernels (sv_kernels.cu).
+//
+// A circuit is executed as a sequence of *passes*.  A pass streams the whole
+// state once through HBM in tiles of 2^m amplitudes: the tile of a pass is
+// the set of amplitudes that differ only in the pass's m "tile bits" (the
+// lowest ``c`` bits of the flat index are always tile bits so every tile is
+// made of 2^c-amplitude contiguous runs).  Inside a tile, the gates of the
+// pass run in *phases*: in a phase every thread holds 2^R amplitudes in
+// registers -- the amplitudes that differ in the phase's R register bits --
+// and applies all gates of the phase to them without touching shared memory.
+// Between phases the tile is re-read from shared memory with another choice
+// of register bits.
+//
+// Everything a kernel needs about one pass travels in one PassParams struct
+// passed by value (``__grid_constant__``); the program needs no device memory.
+#pragma once
+#include <stdint.h>
+
+namespace tedq {
+
+constexpr int kMaxPhases = 24;
+constexpr int kMaxPassGates = 160;
+constexpr int kMaxMats = 128;
+constexpr int kMaxFactors = 192;
+constexpr int kMaxFixed = 96;
+constexpr int kMaxTileBits = 16;
+constexpr int kMaxStateBits = 34;
+constexpr int kMaxRegUnits = 32;
+constexpr int kMaxTidBits = 16;
+
+// Register-phase gate kinds.
+enum GateKind : uint8_t {
+  GK_U1 = 0,    // dense 2x2 on register bit k0 (matrix: 4 entries)
+  GK_D1 = 1,    // diagonal 2x2 on k0 (matrix: 2 entries)
+  GK_X = 2,     // controlled bit flip of k0 (no matrix)
+  GK_SWAP = 3,  // swap of register bits k0, k1 (no matrix)
+};
+
+// Generator kinds of the adjoint gradient: the gradient of a gate
+// U(theta) with dU/dtheta = K U is 2 Re <lambda| K |psi> evaluated on the
+// states after the gate.  K = -i/2 sigma (rotations) or i P1 (phases);
+// the kernel returns coef * Im <lambda| G |psi> restricted to the control
+// subspace with G = X, Y, Z or P1 = |1><1|.
+enum GradKind : uint8_t { GR_NONE = 0, GR_X = 1, GR_Y = 2, GR_Z = 3, GR_P1 = 4 };
+
+struct RGate {
+  uint8_t kind;    // GateKind
+  uint8_t k0, k1;  // register bit indices
+  uint8_t cmask;   // controls (register-bit mask); all must be 1
+  uint8_t mat;     // index into PassParams::mat
+  uint8_t grad;    // GradKind (adjoint only)
+  uint8_t pad[2];
+  int32_t slot;    // parameter slot receiving the gradient, -1 = none
+  float coef;      // gradient coefficient
+};
+
+// Factor ops: one factor produces a 2x2 matrix (dense or diagonal).
+enum FactorOp : uint8_t {
+  F_FIXED2 = 0,  // fixed dense 2x2 at fixed[fix .. fix+3]
+  F_FIXD = 1,    // fixed diagonal at fixed[fix .. fix+1]
+  F_RX = 2, F_RY = 3, F_RZ = 4, F_PHASE = 5, F_ROT = 6,
+};
+
+struct Factor {
+  uint8_t op;
+  uint8_t pad;
+  int16_t fix;
+  int32_t slot[3];  // parameter slots, -1 = use val
+  double val[3];
+};
+
+// A matrix of a pass: the product F_last ... F_first of its factors.
+struct MatDesc {
+  uint8_t diag;    // 1: the product is diagonal (2 entries), 0: dense 2x2
+  uint8_t nf;      // number of factors
+  uint8_t f0;      // first factor index
+  uint8_t dagger;  // 1: use the conjugate transpose (adjoint sweep)
+};
+
+struct CD { double re, im; };
+
+enum PhaseType : uint8_t { PH_REG = 0, PH_DENSE = 1 };
+
+struct Phase {
+  uint8_t type;       // PhaseType
+  uint8_t ntid;       // tid bits used for this phase's tile positions
+  uint16_t g0, g1;    // RGate range [g0, g1) (PH_REG)
+  // PH_REG: shared-memory unit offset (swizzled) of register unit j and of
+  // thread-index bit b; unit address = XOR of the tid offsets ^ reg_off[j].
+  uint16_t reg_off[kMaxRegUnits];
+  uint16_t tid_off[kMaxTidBits];
+  // PH_DENSE: one fixed k-qubit matrix applied directly in shared memory.
+  uint8_t dk;          // 1..3
+  uint8_t dpos[3];     // tile positions, dpos[0] = most significant matrix bit
+  uint16_t dcmask;     // control mask over tile positions
+  uint8_t dagger;
+  uint8_t pad;
+  uint16_t dfix;       // first entry in fixed[] (4^dk entries, row-major)
+  uint16_t pad2;
+};
+
+struct PassParams {
+  uint8_t m;        // tile bits
+  uint8_t c;        // low contiguous tile bits (chunk = 2^c amplitudes)
+  uint8_t e;        // amplitudes per 16-byte unit = 2^e (1 for c64, 0 for c128)
+  uint8_t R;        // register bits
+  uint8_t n;        // state bits
+  uint8_t n_outer;  // n - m
+  uint8_t n_phases;
+  uint8_t init;     // first pass of a forward sweep: 0 = read psi,
+                    // 1 = generate |0..0>, 2 = read the shared initial state
+  uint16_t n_gates, n_mats, n_factors, n_grad;
+  uint8_t pad_bits;  // init == 2: low idle qubits added by padding
+  uint8_t lam_init;  // adjoint: first pass builds lambda from psi in-kernel
+  uint8_t pad[2];
+  uint8_t hi[kMaxTileBits];      // global bit of tile bit c+i
+  uint8_t outer[kMaxStateBits];  // global bit of outer-index bit i
+  Phase phase[kMaxPhases];
+  RGate gate[kMaxPassGates];
+  MatDesc mat[kMaxMats];
+  Factor factor[kMaxFactors];
+  CD fixed[kMaxFixed];
+};
+
+// Unit-level shared-memory swizzle: the 16-byte unit u of a tile is stored at
+// u ^ fold3(u >> 3) where fold3 xors the 3-bit groups.  The map is linear over
+// GF(2), so offsets of disjoint bit sets combine with XOR.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline uint32_t swz_unit(uint32_t u) {
+  uint32_t v = u >> 3, f = 0;
+  while (v) { f ^= v & 7u; v >>= 3; }
+  return u ^ f;
+}
+
+}  // namespace tedq

@@ -1,0 +1,20 @@
+"""tedq_gb300 -- GB300 (sm_103a) execution backend for TeD-Q compiled circuits.
+
+The circuit-recording API mirrors the reference's ``tedq`` package
+(``Circuit``, the gate/observable classes, ``expval``/``probs``/``state``) so
+circuits written for TeD-Q run unchanged with ``import tedq_gb300 as qai`` and
+``circuit.compilecircuit(backend="gb300")``.  ``register_with_tedq()`` adds the
+same backend string to an installed reference ``tedq``.
+"""
+
+from .circuit import Circuit, generate_parameters  # noqa: F401
+from .errors import BackendError, QuantumCircuitError, QuantumStorageError, QuantumValueError  # noqa: F401
+from .measurement import (Expectation, MeasurementReturnTypes, Probability, QuantumMeasurement,  # noqa: F401
+                          State, expval, probs, sample, state, var)
+from .operators import (CNOT, CRX, CRY, CRZ, CSWAP, CY, CZ, RX, RY, RZ, SWAP, SX, ControlledPhaseShift,  # noqa: F401
+                        GateBase, Hadamard, I, IintStateVector, ObservableBase, OperatorBase, PauliX, PauliY,
+                        PauliZ, PhaseShift, Rot, S, T, Toffoli, Unitary)
+from .backend import GB300Backend, GB300Execute, GB300ParamShift  # noqa: F401
+from .reference_bridge import register_with_tedq  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,612 @@
+"""``GB300Backend``: the GB300 execution backend behind ``compilecircuit``.
+
+Drop-in for the reference's ``PyTorchBackend`` (tedq/backends/
+pytorch_backend.py:44-165) and its base ``CompiledCircuit``
+(tedq/backends/compiled_circuit.py:34-647):
+
+* constructed as ``GB300Backend(backend, circuit, **kwargs)`` with the same
+  keyword arguments (``use_cotengra``, ``use_jdopttn``, ``tn_mode``,
+  ``hyper_opt``, ``tn_simplify``, ``requires_grad``, ``interface``,
+  ``diff_method``) plus ``precision`` ("c64" | "c128") and ``fuse``;
+* called as ``compiled(*params)`` with torch tensors; parameters are flattened
+  and bound positionally to the trainable slots in gate order
+  (compiled_circuit.py:492-547); the result is ``torch.stack`` of the
+  measurement results (pytorch_backend.py:385-389);
+* differentiable through ``GB300Execute`` (a ``torch.autograd.Function``)
+  whose backward is the native adjoint sweep -- the replacement of
+  ``back_prop`` -- or, with ``diff_method="param_shift"``, through
+  ``GB300ParamShift`` which evaluates the shifted circuits of
+  ``jacobian_param_shift`` (pytorch_backend.py:180-212) as one batch.
+
+All numerical work runs in ``libtedq_gb300.so`` on the GPU; tensors on the
+host are copied to the current CUDA device and results are returned on the
+parameters' device.
+"""
+
+import ctypes
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from . import _lib
+from .operators import CONTROL_SHIFT_RECIPE, DEFAULT_SHIFT_RECIPE
+
+_CONTROLLED_ROTATIONS = ("CRX", "CRY", "CRZ")
+
+
+def _kind(meas):
+    rt = meas.return_type
+    return rt.value if hasattr(rt, "value") else str(rt)
+
+
+def _as_float(x):
+    if isinstance(x, torch.Tensor):
+        return float(x.detach().reshape(-1)[0])
+    return float(np.asarray(x).reshape(-1)[0])
+
+
+def _cmatrix(m, k):
+    a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).reshape(2 ** k, 2 ** k))
+    return np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1).reshape(-1))
+
+
+class NativeProgram:
+    """Owner of one ``tedq_program_t`` (compile of a recorded circuit)."""
+
+    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0):
+        L = _lib.lib()
+        self.n = int(circuit.num_qubits)
+        ops = list(circuit.operators)
+        gates = (_lib.Gate * max(1, len(ops)))()
+        self._keep = []
+        slot = 0
+        self.slot_of = []  # per operator: list of (param position, slot)
+        for i, op in enumerate(ops):
+            g = gates[i]
+            name = op.name
+            inv = name.endswith(".inv")
+            base = name[:-4] if inv else name
+            qs = list(op.qubits)
+            if not 1 <= len(qs) <= 3:
+                raise NotImplementedError(f"{name}: gates on {len(qs)} qubits are not supported")
+            g.n_qubits = len(qs)
+            for j, q in enumerate(qs):
+                g.qubits[j] = int(q)
+            for j in range(3):
+                g.param_slot[j] = -1
+            tp = list(op.trainable_params)
+            slots = []
+            if tp:
+                if inv or base not in _lib.OP:
+                    raise NotImplementedError(f"{name}: trainable parameters on this gate are not supported")
+                g.op = _lib.OP[base]
+                for j, p in enumerate(op.parameters):
+                    g.fixed[j] = _as_float(p)
+                for pos in tp:
+                    g.param_slot[pos] = slot
+                    slots.append((pos, slot))
+                    slot += 1
+            elif base in _lib.OP and op.num_params == 0 and not inv:
+                g.op = _lib.OP[base]
+            else:
+                # the reference applies the recorded matrix of gates without
+                # trainable parameters (compiled_circuit.py:432-435)
+                g.op = _lib.OP_MATRIX
+                arr = _cmatrix(op.matrix, len(qs))
+                self._keep.append(arr)
+                g.matrix = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            self.slot_of.append(slots)
+        self.n_params = slot
+        meas = list(circuit.measurements)
+        M = (_lib.Meas * max(1, len(meas)))()
+        self.layout = []  # per measurement: ("expval", k) | ("probs", off, nq) | ("state",)
+        k_real = 0
+        for i, m in enumerate(meas):
+            kind = _kind(m)
+            if kind == "expval":
+                obs = m.obs if isinstance(m.obs, list) else [m.obs]
+                F = (_lib.ObsFactor * len(obs))()
+                for j, ob in enumerate(obs):
+                    qs = list(ob.qubits)
+                    F[j].n_qubits = len(qs)
+                    for t, q in enumerate(qs):
+                        F[j].qubits[t] = int(q)
+                    if ob.name in _lib.OBS and len(qs) == 1:
+                        F[j].obs = _lib.OBS[ob.name]
+                    else:
+                        F[j].obs = _lib.OBS_MATRIX
+                        arr = _cmatrix(ob.matrix, len(qs))
+                        self._keep.append(arr)
+                        F[j].matrix = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                self._keep.append(F)
+                M[i].kind = _lib.MEAS_EXPVAL
+                M[i].n_factors = len(obs)
+                M[i].factors = F
+                self.layout.append(("expval", k_real))
+                k_real += 1
+            elif kind == "probs":
+                M[i].kind = _lib.MEAS_PROBS
+                if m.qubits is None:
+                    M[i].n_qubits = 0
+                    nq = self.n
+                else:
+                    qs = [int(q) for q in m.qubits]
+                    arr = (ctypes.c_int32 * max(1, len(qs)))(*qs)
+                    self._keep.append(arr)
+                    M[i].n_qubits = len(qs)
+                    M[i].qubits = arr
+                    nq = len(set(qs))
+                    if len(qs) == 0:
+                        raise ValueError("probs(qubits=[]) has no outcome")
+                self.layout.append(("probs", k_real, nq, m))
+                k_real += 2 ** nq
+            elif kind == "state":
+                M[i].kind = _lib.MEAS_STATE
+                self.layout.append(("state",))
+            else:
+                raise NotImplementedError(f"measurement {kind} is not implemented")
+        opts = _lib.Options()
+        opts.precision = _lib.PREC_C128 if precision == "c128" else _lib.PREC_C64
+        opts.fuse = 1 if fuse else 0
+        opts.tile_qubits = int(tile_qubits)
+        h = ctypes.c_void_p()
+        _lib.check(L.tedq_program_create(gates, len(ops), self.n, M, len(meas), ctypes.byref(opts), ctypes.byref(h)),
+                   "tedq_program_create")
+        self.handle = h
+        info = _lib.ProgramInfo()
+        _lib.check(L.tedq_program_info(h, ctypes.byref(info)), "tedq_program_info")
+        self.info = info
+        self.ns = info.state_qubits
+        self.pad = self.ns - self.n
+        self.n_real = info.n_real_outputs
+        if info.n_params != self.n_params:
+            raise RuntimeError(f"native program has {info.n_params} parameter slots, expected {self.n_params}")
+        self.precision = precision
+        self.rdtype = torch.float64 if precision == "c128" else torch.float32
+        self.cdtype = torch.complex128 if precision == "c128" else torch.complex64
+        self.has_state = any(x[0] == "state" for x in self.layout)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.tedq_program_destroy(h)
+            self.handle = None
+
+    def describe(self, adjoint=False):
+        import json
+        L = _lib.lib()
+        need = L.tedq_program_describe(self.handle, int(adjoint), None, 0)
+        buf = ctypes.create_string_buffer(int(need))
+        L.tedq_program_describe(self.handle, int(adjoint), buf, need)
+        return json.loads(buf.value.decode())
+
+    def workspace_bytes(self, batch):
+        return int(_lib.lib().tedq_program_workspace_bytes(self.handle, int(batch)))
+
+
+class _Workspace:
+    """Grow-only device scratch shared by the calls of one backend."""
+
+    def __init__(self):
+        self.buf = None
+
+    def get(self, nbytes, device):
+        if nbytes <= 0:
+            return None, 0
+        if self.buf is None or self.buf.numel() < nbytes or self.buf.device != device:
+            self.buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=device)
+        ptr = self.buf.data_ptr()
+        off = (-ptr) % 256
+        return ptr + off, self.buf.numel() - off
+
+
+def _stream_ptr(device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class GB300Execute(torch.autograd.Function):
+    """Batched forward with the adjoint-method backward.
+
+    Same ``(None, *grads)`` convention as the reference's ``TorchExecute``
+    (pytorch_backend.py:1191-1223); the backward is one native adjoint sweep
+    instead of 2P shifted re-executions or an autograd graph of every gate."""
+
+    @staticmethod
+    def forward(ctx, backend, P):
+        out, psi = backend._forward(P)
+        ctx.backend = backend
+        ctx.save_for_backward(P)
+        ctx.psi = psi
+        ctx.consumed = False
+        if out is None:
+            out = P.new_zeros((P.shape[0], 0))
+        if backend._prog.has_state:
+            return out, psi
+        st = psi.new_empty(0)
+        ctx.mark_non_differentiable(st)
+        return out, st
+
+    @staticmethod
+    def backward(ctx, d_out, d_state):
+        (P,) = ctx.saved_tensors
+        b = ctx.backend
+        if ctx.consumed:
+            _, psi = b._forward(P.detach())
+        elif b._prog.has_state:
+            psi = ctx.psi.clone()
+        else:
+            psi = ctx.psi
+            ctx.consumed = True
+        if d_state is not None and d_state.numel() == 0:
+            d_state = None
+        grad = b._adjoint(P.detach(), psi, d_out, d_state)
+        return None, grad
+
+
+class GB300ParamShift(torch.autograd.Function):
+    """Forward as ``GB300Execute``; backward by the parameter-shift rule.
+
+    The shifted evaluations of ``jacobian_param_shift`` (pytorch_backend.py
+    :180-212; recipes ops_abc.py:261-280, qubit.py:32-42) run as one batch."""
+
+    @staticmethod
+    def forward(ctx, backend, P):
+        out, psi = backend._forward(P)
+        ctx.backend = backend
+        ctx.save_for_backward(P)
+        if out is None:
+            out = P.new_zeros((P.shape[0], 0))
+        st = psi if backend._prog.has_state else psi.new_empty(0)
+        if not backend._prog.has_state:
+            ctx.mark_non_differentiable(st)
+        return out, st
+
+    @staticmethod
+    def backward(ctx, d_out, d_state):
+        (P,) = ctx.saved_tensors
+        b = ctx.backend
+        if b._prog.has_state and d_state is not None and d_state.abs().sum() > 0:
+            raise NotImplementedError("param_shift differentiation of state outputs is not supported")
+        jac = b.jacobian_param_shift(P.detach())  # [B, n_real, n_params]
+        grad = torch.einsum("bk,bkp->bp", d_out.to(jac.dtype), jac)
+        return None, grad.to(P.dtype)
+
+
+class GB300Backend:
+    """Compiled circuit executed by the GB300 library (see module docstring)."""
+
+    def __init__(self, backend, circuit, use_cotengra=False, use_jdopttn=False, tn_mode=False, hyper_opt=None,
+                 tn_simplify=True, **kwargs):
+        # argument checks of CompiledCircuit.__init__ (compiled_circuit.py:58-67)
+        if use_cotengra and use_jdopttn:
+            raise ValueError("Error!!!! can not use contengra, opt_einsum and cyc at the same time!")
+        if (use_cotengra or use_jdopttn) and tn_mode:
+            raise ValueError("Error!!!! can not use contengra, opt_einsum and cyc at the same time!")
+        self._backend = backend
+        self._circuit = circuit
+        self._use_cotengra = use_cotengra
+        self._use_jdopttn = use_jdopttn
+        self._tn_mode = tn_mode
+        self._hyper_opt = hyper_opt
+        self._tn_simplify = tn_simplify
+        self._calculation_mode = False
+        self._requires_grad = kwargs.get("requires_grad", True)
+        self._interface = kwargs.get("interface", "pytorch")
+        self._diff_method = kwargs.get("diff_method", "back_prop")
+        self._precision = kwargs.get("precision", "c64")
+        if self._interface != "pytorch":
+            raise ValueError(f"{self._interface}: pytroch_backend only supports pytorch interface!")
+        if self._precision not in ("c64", "c128"):
+            raise ValueError(f"{self._precision}: precision must be 'c64' or 'c128'")
+        self._num_qubits = circuit.num_qubits
+        self._operators = OrderedDict()
+        self._operatorname = OrderedDict()
+        self._appliedqubits = OrderedDict()
+        self._operatorparams = OrderedDict()
+        self._trainableparams = OrderedDict()
+        for op in circuit.operators:
+            self._operators[op.instance_id] = op
+            self._operatorname[op.instance_id] = op.name
+            self._appliedqubits[op.instance_id] = op.qubits
+            self._operatorparams[op.instance_id] = op.parameters
+            self._trainableparams[op.instance_id] = op.trainable_params
+        self._measurements = circuit.measurements
+        self._init_state = circuit.init_state
+        self._prog = NativeProgram(circuit, self._precision, fuse=kwargs.get("fuse", True),
+                                   tile_qubits=kwargs.get("tile_qubits", 0))
+        self._ws = _Workspace()
+        self._device = None
+        self._init_dev = None
+        self._states_after_measurement = None
+
+    # ------------------------------------------------------------ properties
+    @property
+    def operators(self):
+        return list(self._operators.values())
+
+    @property
+    def gates_names(self):
+        return list(self._operatorname.values())
+
+    @property
+    def gate_parameters(self):
+        return list(self._operatorparams.values())
+
+    @property
+    def parameters(self):
+        out = []
+        for pars in self._operatorparams.values():
+            out.extend(pars)
+        return out
+
+    @property
+    def trainable_parameters(self):
+        out = []
+        for idx, tp in self._trainableparams.items():
+            for i in tp:
+                out.append(self._operatorparams[idx][i])
+        return out
+
+    @property
+    def qubits(self):
+        return list(self._appliedqubits.values())
+
+    @property
+    def interface(self):
+        return self._interface
+
+    @property
+    def diff_method(self):
+        return self._diff_method
+
+    @property
+    def backend(self):
+        return self._backend
+
+    @property
+    def measurements(self):
+        return self._measurements
+
+    @property
+    def calculation_mode(self):
+        return self._calculation_mode
+
+    @property
+    def device(self):
+        return self._device
+
+    @property
+    def num_params(self):
+        return self._prog.n_params
+
+    @property
+    def program_info(self):
+        i = self._prog.info
+        return {f: getattr(i, f) for f, _ in i._fields_ if f != "reserved"}
+
+    def describe(self, adjoint=False):
+        return self._prog.describe(adjoint)
+
+    @property
+    def states_after_measurement(self):
+        if self._states_after_measurement is None:
+            raise ValueError("no states after measurement found! please measure probs with qubits.")
+        return self._states_after_measurement
+
+    # ------------------------------------------------------------ execution
+    def _exec_device(self, params):
+        """Same-device check of check_parameters_torch_device
+        (pytorch_backend.py:85-120); returns the device results go to."""
+        the_same = None
+        for par in params:
+            try:
+                index = par.device.index if par.is_cuda else -1
+            except AttributeError as error:
+                raise ValueError("input parameters must be type of pytorch tensor!!") from error
+            if the_same is None:
+                the_same = index
+            if the_same != index:
+                raise ValueError("input parameters are not in the same device!!")
+        self._device = params[0].device if params else None
+        return self._device
+
+    @staticmethod
+    def _cuda_device(dev):
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 backend needs a CUDA device (none is available)")
+        if dev is not None and dev.type == "cuda":
+            return dev
+        return torch.device("cuda", torch.cuda.current_device())
+
+    def _init_tensor(self, dev):
+        if self._init_state is None:
+            return None
+        if self._init_dev is None or self._init_dev.device != dev:
+            v = np.asarray(self._init_state.matrix).reshape(-1)
+            self._init_dev = torch.as_tensor(v, dtype=self._prog.cdtype).to(dev).contiguous()
+        return self._init_dev
+
+    def _forward(self, P):
+        """Native forward on a [B, n_params] parameter tensor on a CUDA device."""
+        prog = self._prog
+        dev = P.device
+        B = P.shape[0]
+        P = P.to(prog.rdtype).contiguous()
+        psi = torch.empty((B, 1 << prog.ns), dtype=prog.cdtype, device=dev)
+        out = torch.empty((B, prog.n_real), dtype=prog.rdtype, device=dev) if prog.n_real else None
+        ws, wsb = self._ws.get(prog.workspace_bytes(B), dev)
+        init = self._init_tensor(dev)
+        L = _lib.lib()
+        self._last_psi = psi
+        with torch.cuda.device(dev):
+            _lib.check(L.tedq_run(prog.handle, ctypes.c_void_p(P.data_ptr() if P.numel() else 0), B,
+                                  ctypes.c_void_p(psi.data_ptr()),
+                                  ctypes.c_void_p(out.data_ptr() if out is not None else 0),
+                                  ctypes.c_void_p(init.data_ptr() if init is not None else 0),
+                                  ctypes.c_void_p(ws or 0), wsb, _stream_ptr(dev)), "tedq_run")
+        return out, psi
+
+    def _adjoint(self, P, psi, d_out, d_state):
+        prog = self._prog
+        dev = P.device
+        B = P.shape[0]
+        P = P.to(prog.rdtype).contiguous()
+        lam = torch.empty_like(psi)
+        grad = torch.empty((B, prog.n_params), dtype=prog.rdtype, device=dev)
+        dy = d_out.to(prog.rdtype).contiguous() if (d_out is not None and d_out.numel()) else None
+        ds = d_state.to(prog.cdtype).contiguous() if d_state is not None else None
+        ws, wsb = self._ws.get(prog.workspace_bytes(B), dev)
+        L = _lib.lib()
+        with torch.cuda.device(dev):
+            _lib.check(L.tedq_run_adjoint(prog.handle, ctypes.c_void_p(P.data_ptr()), B,
+                                          ctypes.c_void_p(dy.data_ptr() if dy is not None else 0),
+                                          ctypes.c_void_p(ds.data_ptr() if ds is not None else 0),
+                                          ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(lam.data_ptr()),
+                                          ctypes.c_void_p(grad.data_ptr()), ctypes.c_void_p(ws or 0), wsb,
+                                          _stream_ptr(dev)), "tedq_run_adjoint")
+        return grad
+
+    def _assemble(self, out, psi):
+        """Reference-shaped results [B, M, ...] from the native outputs."""
+        prog = self._prog
+        B = psi.shape[0]
+        res = []
+        for item in prog.layout:
+            if item[0] == "expval":
+                res.append(out[:, item[1]])
+            elif item[0] == "probs":
+                res.append(out[:, item[1]:item[1] + 2 ** item[2]].reshape([B] + [2] * item[2]))
+            else:
+                st = psi if prog.pad == 0 else psi[:, :: (1 << prog.pad)]
+                res.append(st.reshape([B] + [2] * prog.n))
+        shapes = {tuple(r.shape) for r in res}
+        if len(shapes) != 1:
+            raise ValueError("You can not have multiple measurements with different shapes!!")
+        return torch.stack(res, 1)
+
+    def _flatten(self, params):
+        if not params:
+            return torch.zeros(0)
+        return torch.cat([p.reshape(-1) for p in params])
+
+    def _bind_for_properties(self, flat_rows):
+        """Positional update of the recorded parameter lists (compiled_circuit.py:522-547)."""
+        count = 0
+        for idx, tp in self._trainableparams.items():
+            for i, pos in enumerate(tp):
+                self._operatorparams[idx][pos] = flat_rows[count + i]
+            count += len(tp)
+
+    def __call__(self, *params):
+        dev = self._exec_device(params)
+        flat = self._flatten(params)
+        P = self._prog.n_params
+        if flat.numel() != P:
+            raise ValueError(f"Error!!!! number of parameters are not matched!! required {P} but {flat.numel()} "
+                             f"are given")
+        if self._diff_method == "param_shift" and self._requires_grad:
+            dts = [p.dtype for p in params]
+            if any(d != dts[0] for d in dts):
+                raise ValueError("input parameters for parameter shift method must have the same data type!")
+        if self._diff_method == "finite_diff" and self._requires_grad:
+            raise NotImplementedError
+        if self._diff_method not in ("back_prop", "adjoint", "param_shift", "finite_diff") and self._requires_grad:
+            raise Exception(f"Differentiation method {self._diff_method} is not supported. "
+                            f"Supported methods include {{back_prop, adjoint, param_shift}}")
+        if P and len(self._operatorparams) and P <= 4096:
+            self._bind_for_properties(list(flat.reshape(-1, 1)))
+        result = self.execute_batch(flat.reshape(1, -1))[0]
+        if any(item[0] == "probs" and getattr(item[3], "after_state", False) and item[3].qubits is not None
+               for item in self._prog.layout):
+            self._record_after_states()
+        return result.to(dev) if dev is not None else result
+
+    def execute_batch(self, params):
+        """Evaluate B parameter vectors at once: ``params`` [B, n_params] ->
+        results [B, M, ...] (a native batch dimension; the reference has none)."""
+        if params.dim() != 2 or params.shape[1] != self._prog.n_params:
+            raise ValueError(f"execute_batch expects [B, {self._prog.n_params}] parameters, got "
+                             f"{tuple(params.shape)}")
+        cdev = self._cuda_device(params.device)
+        Pc = params.to(cdev)
+        if not self._requires_grad:
+            with torch.no_grad():
+                out, psi = self._forward(Pc.detach())
+                return self._assemble(out, psi)
+        fn = GB300ParamShift if self._diff_method == "param_shift" else GB300Execute
+        out, st = fn.apply(self, Pc)
+        return self._assemble(out, st if st.numel() else _PsiShape(out.shape[0], self._prog))
+
+    # ------------------------------------------------------------ gradients
+    def jacobian_param_shift(self, P):
+        """[B, n_real, n_params] Jacobian by the parameter-shift rule; all
+        shifted circuits of a batch run as one native batch."""
+        prog = self._prog
+        B, n = P.shape
+        rows, plan = [], []
+        for idx, tp in self._trainableparams.items():
+            op = self._operators[idx]
+            recipe = CONTROL_SHIFT_RECIPE if op.name in _CONTROLLED_ROTATIONS else DEFAULT_SHIFT_RECIPE
+            for _ in tp:
+                plan.append(recipe)
+        shifted = []
+        for j, recipe in enumerate(plan):
+            for c, a, s in recipe:
+                Q = a * P.clone()
+                Q[:, j] += s
+                shifted.append(Q)
+        if not shifted:
+            return P.new_zeros((B, prog.n_real, 0))
+        Q = torch.stack(shifted, 0).reshape(-1, n)  # [T*B, n]
+        with torch.no_grad():
+            out, _ = self._forward(Q)
+        out = out.reshape(len(shifted), B, prog.n_real)
+        jac = P.new_zeros((B, prog.n_real, n), dtype=out.dtype)
+        t = 0
+        for j, recipe in enumerate(plan):
+            for c, a, s in recipe:
+                jac[:, :, j] += c * out[t]
+                t += 1
+        return jac
+
+    def finite_diff_jacobian(self, P, eps=1e-3):
+        """Central finite differences [B, n_real, n_params] (a checking aid)."""
+        B, n = P.shape
+        Q = torch.cat([P.unsqueeze(0) + eps * torch.eye(n, dtype=P.dtype, device=P.device).unsqueeze(1),
+                       P.unsqueeze(0) - eps * torch.eye(n, dtype=P.dtype, device=P.device).unsqueeze(1)], 0)
+        with torch.no_grad():
+            out, _ = self._forward(Q.reshape(-1, n))
+        out = out.reshape(2, n, B, -1)
+        return ((out[0] - out[1]) / (2 * eps)).permute(1, 2, 0)
+
+    def _record_after_states(self):
+        """``states_after_measurement`` of a probs measurement with
+        ``after_state=True`` (pytorch_backend.py:474-493)."""
+        psi = getattr(self, "_last_psi", None)
+        if psi is None:
+            return
+        prog = self._prog
+        st = (psi if prog.pad == 0 else psi[:, :: (1 << prog.pad)])[0].reshape([2] * prog.n).detach()
+        for item in prog.layout:
+            if item[0] != "probs" or not getattr(item[3], "after_state", False) or item[3].qubits is None:
+                continue
+            qubits = list(item[3].qubits)
+            out = {}
+            for i in range(2 ** len(qubits)):
+                bits = [int(b) for b in format(i, f"0{len(qubits)}b")]
+                sel = dict(zip(qubits, bits))
+                sub = st[tuple(sel.get(ax, slice(None)) for ax in range(prog.n))]
+                scale = torch.sqrt(torch.sum(torch.abs(sub) ** 2))
+                out["".join(str(b) for b in bits)] = [s / scale for s in sub]
+            self._states_after_measurement = out
+
+
+class _PsiShape:
+    """Placeholder standing in for the state when no state is measured."""
+
+    def __init__(self, B, prog):
+        self.shape = (B, 1 << prog.ns)
+
+    def __getitem__(self, item):
+        raise RuntimeError("state output requested from a program without state measurement")

@@ -1,0 +1,159 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden
+vectors and the CPU oracle.
+
+Tolerances: complex64 results within 1e-5 (absolute on expvals bounded by 1,
+relative 1e-5); complex128 within 1e-12; gradients of the complex64 path
+within 2e-5 of the complex128 reference.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import load_cases
+
+pytestmark = pytest.mark.gpu
+
+qai = pytest.importorskip("tedq_gb300")
+CASES = load_cases()
+DEV = "cuda:0"
+
+
+def _arr(v):
+    a = np.asarray(v, dtype=np.float64)
+    if a.ndim == 2 and a.shape[1] == 2:
+        return a[:, 0] + 1j * a[:, 1]
+    return a
+
+
+def _compile(case, precision, **kw):
+    return qai.Circuit.from_spec(case).compilecircuit(backend="gb300", precision=precision, **kw)
+
+
+def _rdt(precision):
+    return torch.float64 if precision == "c128" else torch.float32
+
+
+@pytest.fixture(autouse=True)
+def _native_loaded():
+    yield
+    assert qai._lib._lib is not None, "native library was not used"
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_forward_matches_reference(case, precision):
+    cc = _compile(case, precision)
+    p = torch.tensor(case["params"], dtype=_rdt(precision), device=DEV)
+    out = cc(p) if case["params"] else cc()
+    assert list(out.shape) == case["shape"]
+    got = out.detach().cpu().numpy().reshape(-1)
+    if precision == "c64":
+        np.testing.assert_allclose(got, _arr(case["out_c64"]), atol=1e-5, rtol=1e-5)
+        np.testing.assert_allclose(got, _arr(case["out_c128"]), atol=1e-5, rtol=1e-5)
+    else:
+        np.testing.assert_allclose(got, _arr(case["out_c128"]), atol=1e-12, rtol=1e-12)
+
+
+GRAD_CASES = [c for c in CASES if c["params"]]
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+@pytest.mark.parametrize("case", GRAD_CASES, ids=[c["name"] for c in GRAD_CASES])
+def test_adjoint_grad_matches_backprop(case, precision):
+    cc = _compile(case, precision)
+    p = torch.tensor(case["params"], dtype=_rdt(precision), device=DEV, requires_grad=True)
+    out = cc(p)
+    dy = torch.tensor(case["dy"], dtype=torch.float64, device=DEV).reshape(out.shape)
+    loss = (out * dy.to(out.dtype)).real.sum() if out.is_complex() else (out * dy.to(out.dtype)).sum()
+    loss.backward()
+    g = p.grad.cpu().numpy()
+    if precision == "c64":
+        np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=2e-5, rtol=2e-5)
+    else:
+        np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=1e-11, rtol=1e-10)
+
+
+PS_CASES = [c for c in CASES if "grad_paramshift_c64" in c]
+
+
+@pytest.mark.parametrize("case", PS_CASES, ids=[c["name"] for c in PS_CASES])
+def test_param_shift_matches_reference(case):
+    cc = _compile(case, "c64", diff_method="param_shift")
+    p = torch.tensor(case["params"], dtype=torch.float32, device=DEV, requires_grad=True)
+    out = cc(p)
+    out.backward(torch.tensor(case["dy"], dtype=torch.float32, device=DEV).reshape(out.shape))
+    np.testing.assert_allclose(p.grad.cpu().numpy(), case["grad_paramshift_c64"], atol=2e-5, rtol=2e-5)
+
+
+def test_reference_test_goldens_literal():
+    """The values hard-coded in the reference's tests (test_pytorch_backend.py:386-553)."""
+    def circuit_def(*params):
+        qai.RX(params[0], qubits=[0])
+        qai.RY(params[1], qubits=[0])
+        return [qai.expval(qai.PauliZ(qubits=[0])), qai.expval(qai.PauliX(qubits=[1]))]
+    for method in ("back_prop", "param_shift"):
+        a = torch.tensor([0.54], requires_grad=True)
+        b = torch.tensor([0.12], requires_grad=True)
+        cc = qai.Circuit(circuit_def, 2, a, b).compilecircuit(backend="gb300", diff_method=method)
+        res = cc(a, b)
+        assert res.device.type == "cpu"
+        assert np.array_equal(np.round(res.detach().numpy(), 5), np.round(np.array([0.85154057, 0.0], np.float32), 5))
+        res[0].backward()
+        assert np.round(a.grad.numpy(), 5) == np.round(np.float32(-0.5104387), 5)
+        assert np.round(b.grad.numpy(), 5) == np.round(np.float32(-0.10267819), 5)
+
+
+def _vqc_spec(n, layers, seed):
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers):
+        for q in range(n):
+            for name in ("RX", "RY", "RZ"):
+                gates.append({"name": name, "qubits": [q], "params": [float(rng.uniform(0, 2 * np.pi))],
+                              "trainable": [0]})
+        for q in range(n - 1):
+            gates.append({"name": "CNOT", "qubits": [q, q + 1], "params": [], "trainable": []})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
+    meas.append({"kind": "expval", "list": True,
+                 "obs": [{"name": "PauliZ", "qubits": [0]}, {"name": "PauliZ", "qubits": [1]}]})
+    return {"n": n, "gates": gates, "meas": meas, "init_state": None}
+
+
+@pytest.mark.parametrize("n,layers", [(14, 3), (20, 10)])
+def test_batched_vqc_against_oracle(n, layers):
+    """Multi-pass circuits in a batch, value and adjoint gradient vs the complex128 oracle."""
+    spec = _vqc_spec(n, layers, seed=n)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300")
+    P = cc.num_params
+    gen = torch.Generator().manual_seed(n)
+    params = torch.rand(3, P, generator=gen, dtype=torch.float64) * 2 * np.pi
+    pd = params.to(DEV, torch.float32).requires_grad_(True)
+    out = cc.execute_batch(pd)
+    dy = torch.ones_like(out)
+    (out * dy).sum().backward()
+    for b in (0, 2):
+        want, want_g = oracle.value_and_grad(spec, params[b], np.ones(out.shape[1]), torch.complex128)
+        np.testing.assert_allclose(out[b].detach().cpu().double().numpy(), want.numpy(), atol=1e-5)
+        np.testing.assert_allclose(pd.grad[b].cpu().double().numpy(), want_g.numpy(), atol=5e-5, rtol=1e-4)
+
+
+def test_alone_equals_in_batch():
+    spec = _vqc_spec(12, 2, seed=3)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)
+    params = torch.rand(8, cc.num_params, device=DEV) * 6.28
+    batch = cc.execute_batch(params)
+    for b in (0, 5, 7):
+        alone = cc.execute_batch(params[b:b + 1])
+        torch.testing.assert_close(alone[0], batch[b], atol=1e-6, rtol=1e-6)
+    again = cc.execute_batch(params)
+    torch.testing.assert_close(again, batch, atol=1e-7, rtol=1e-7)
+
+
+def test_unfused_equals_fused():
+    spec = _vqc_spec(11, 2, seed=5)
+    a = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)
+    b = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False, fuse=False)
+    params = torch.rand(4, a.num_params, device=DEV) * 6.28
+    torch.testing.assert_close(a.execute_batch(params), b.execute_batch(params), atol=2e-6, rtol=1e-5)

@@ -1,0 +1,129 @@
+"""CPU checks of the compiled schedule (no GPU): the native compile step runs
+on the host; its exported pass/phase plan is executed by ``plan_interp`` in
+complex128 and compared with the reference's golden outputs and gradients."""
+
+import numpy as np
+import pytest
+import torch
+
+import plan_interp
+from conftest import load_cases
+
+qai = pytest.importorskip("tedq_gb300")
+
+CASES = load_cases()
+
+
+def _arr(v):
+    a = np.asarray(v, dtype=np.float64)
+    if a.ndim == 2 and a.shape[1] == 2:
+        return a[:, 0] + 1j * a[:, 1]
+    return a
+
+
+def _compile(case, precision, fuse=True):
+    circ = qai.Circuit.from_spec(case)
+    return circ.compilecircuit(backend="gb300", precision=precision, fuse=fuse)
+
+
+def _assemble(case, desc, out, psi):
+    pad = desc["state_qubits"] - desc["n"]
+    res = []
+    k = 0
+    for m in case["meas"]:
+        if m["kind"] == "expval":
+            res.append(np.array([out[k]]))
+            k += 1
+        elif m["kind"] == "probs":
+            q = case["n"] if m["qubits"] is None else len(set(m["qubits"]))
+            res.append(out[k:k + 2 ** q])
+            k += 2 ** q
+        else:
+            res.append(psi[:: 1 << pad])
+    return np.concatenate(res)
+
+
+def _init(case):
+    if case.get("init_state") is None:
+        return None
+    return _arr(case["init_state"])
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_plan_forward_matches_reference(case, precision):
+    cc = _compile(case, precision)
+    desc = cc.describe()
+    prm = np.asarray(case["params"], dtype=np.float64)
+    psi = plan_interp.forward(desc, prm, _init(case))
+    got = _assemble(case, desc, plan_interp.outputs(desc, psi), psi)
+    np.testing.assert_allclose(got, _arr(case["out_c128"]), atol=1e-12, rtol=1e-12)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["params"]], ids=[c["name"] for c in CASES if c["params"]])
+def test_plan_adjoint_matches_reference(case):
+    cc = _compile(case, "c128")
+    fwd, bwd = cc.describe(), cc.describe(adjoint=True)
+    prm = np.asarray(case["params"], dtype=np.float64)
+    psi = plan_interp.forward(fwd, prm, _init(case))
+    dy = np.asarray(case["dy"], dtype=np.float64)
+    # split dy into the real outputs and the state outputs, in measurement order
+    dy_real = np.zeros(fwd["n_real"])
+    dy_state = None
+    per = int(np.prod(case["shape"][1:])) if len(case["shape"]) > 1 else 1
+    pad = fwd["state_qubits"] - fwd["n"]
+    k = 0
+    for i, m in enumerate(case["meas"]):
+        chunk = dy[i * per:(i + 1) * per]
+        if m["kind"] == "state":
+            full = np.zeros(psi.size, dtype=complex)
+            full[:: 1 << pad] = chunk
+            dy_state = full if dy_state is None else dy_state + full
+        else:
+            dy_real[k:k + per] = chunk
+            k += per
+    g = plan_interp.adjoint(bwd, prm, psi.copy(), dy_real, dy_state)
+    np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=1e-10, rtol=1e-9)
+
+
+def test_plan_unfused_matches_fused():
+    case = next(c for c in CASES if c["name"] == "all_gates_n4")
+    prm = np.asarray(case["params"], dtype=np.float64)
+    a = plan_interp.forward(_compile(case, "c64", fuse=True).describe(), prm)
+    b = plan_interp.forward(_compile(case, "c64", fuse=False).describe(), prm)
+    np.testing.assert_allclose(a, b, atol=1e-12)
+
+
+def _hea_spec(n, layers, seed):
+    rng = np.random.default_rng(seed)
+    gates = []
+    for _ in range(layers):
+        for q in range(n):
+            for name in ("RX", "RY", "RZ"):
+                gates.append({"name": name, "qubits": [q], "params": [float(rng.uniform(0, 2 * np.pi))],
+                              "trainable": [0]})
+        for q in range(n - 1):
+            gates.append({"name": "CNOT", "qubits": [q, q + 1], "params": [], "trainable": []})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
+    meas.append({"kind": "expval", "list": True, "obs": [{"name": "PauliZ", "qubits": [0]},
+                                                        {"name": "PauliZ", "qubits": [1]}]})
+    return {"n": n, "gates": gates, "meas": meas, "init_state": None}
+
+
+@pytest.mark.parametrize("n,tile", [(14, 0), (15, 11), (16, 10)])
+def test_plan_multi_pass_against_oracle(n, tile):
+    """States larger than one tile: several passes with non-trivial outer bits."""
+    import oracle
+    spec = _hea_spec(n, 2, seed=n)
+    circ = qai.Circuit.from_spec(spec)
+    cc = circ.compilecircuit(backend="gb300", precision="c128", tile_qubits=tile)
+    desc = cc.describe()
+    assert len(desc["passes"]) >= 2
+    prm = np.array([g["params"][0] for g in spec["gates"] if g["trainable"]])
+    psi = plan_interp.forward(desc, prm)
+    want = oracle.run(spec, torch.tensor(prm, dtype=torch.float64), torch.complex128).numpy()
+    np.testing.assert_allclose(plan_interp.outputs(desc, psi), want, atol=1e-12)
+    dy = np.linspace(-1, 1, len(want))
+    g = plan_interp.adjoint(cc.describe(adjoint=True), prm, psi.copy(), dy)
+    _, want_g = oracle.value_and_grad(spec, prm, dy, torch.complex128)
+    np.testing.assert_allclose(g, want_g.numpy(), atol=1e-11)
