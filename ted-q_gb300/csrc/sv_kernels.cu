@@ -205,6 +205,48 @@ __device__ __forceinline__ void apply_d1(cpx<real>* a, const cpx<real>* M, unsig
   }
 }
 
+// RX-type [[c, -i s], [-i s, c]] (RX, or RX^dagger with s negated)
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_rxt(cpx<real>* a, const cpx<real>* M, unsigned cm) {
+  const real c = M[0].x, sn = -M[1].y;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & cm) != cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = mk<real>(fma(c, x0.x, sn * x1.y), fma(c, x0.y, -sn * x1.x));
+    a[j] = mk<real>(fma(c, x1.x, sn * x0.y), fma(c, x1.y, -sn * x0.x));
+  }
+}
+
+// RY-type [[c, -s], [s, c]]
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_ryt(cpx<real>* a, const cpx<real>* M, unsigned cm) {
+  const real c = M[0].x, sn = -M[1].x;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & cm) != cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = mk<real>(fma(c, x0.x, -sn * x1.x), fma(c, x0.y, -sn * x1.y));
+    a[j] = mk<real>(fma(sn, x0.x, c * x1.x), fma(sn, x0.y, c * x1.y));
+  }
+}
+
+// diag(1, d): multiply the |1> half only
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_ph(cpx<real>* a, const cpx<real>* M, unsigned cm) {
+  const cpx<real> d = M[1];
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (!(i & (1 << K))) continue;
+    if ((i & cm) != cm) continue;
+    a[i] = cmul(d, a[i]);
+  }
+}
+
 template <int K, int R, typename real>
 __device__ __forceinline__ void apply_x(cpx<real>* a, unsigned cm) {
 #pragma unroll
@@ -222,9 +264,14 @@ template <int R, typename real, int K = 0>
 __device__ __forceinline__ void dispatch_gate(int kind, int k, cpx<real>* a, const cpx<real>* M, unsigned cm) {
   if constexpr (K < R) {
     if (k == K) {
-      if (kind == GK_U1) apply_u1<K, R, real>(a, M, cm);
-      else if (kind == GK_D1) apply_d1<K, R, real>(a, M, cm);
-      else apply_x<K, R, real>(a, cm);
+      switch (kind) {
+        case GK_U1: apply_u1<K, R, real>(a, M, cm); break;
+        case GK_D1: apply_d1<K, R, real>(a, M, cm); break;
+        case GK_RXT: apply_rxt<K, R, real>(a, M, cm); break;
+        case GK_RYT: apply_ryt<K, R, real>(a, M, cm); break;
+        case GK_PH: apply_ph<K, R, real>(a, M, cm); break;
+        default: apply_x<K, R, real>(a, cm); break;
+      }
     } else {
       dispatch_gate<R, real, K + 1>(kind, k, a, M, cm);
     }
@@ -403,8 +450,15 @@ __global__ void __launch_bounds__(256, 2)
   const real* prm = params ? params + circ * n_params : nullptr;
   for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
   const uint64_t base = tile_base(P, blockIdx.x);
-  const int nunits = 1 << (P.m - E);
-  for (int u = tid; u < nunits; u += T) tile[swz_unit(u)] = load_unit<real>(P, st, unit_global(P, base, u, E), init);
+  // Stage the tile: each thread owns NU units (nunits == NU * T); all global
+  // loads are issued before the first shared-memory store.
+  {
+    U v[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, unit_global(P, base, tid + k * T, E), init);
+#pragma unroll
+    for (int k = 0; k < NU; ++k) tile[swz_unit(tid + k * T)] = v[k];
+  }
   __syncthreads();
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
@@ -436,7 +490,8 @@ __global__ void __launch_bounds__(256, 2)
     __syncthreads();
   }
   U* gst = reinterpret_cast<U*>(st);
-  for (int u = tid; u < nunits; u += T) gst[unit_global(P, base, u, E) >> E] = tile[swz_unit(u)];
+#pragma unroll
+  for (int k = 0; k < NU; ++k) gst[unit_global(P, base, tid + k * T, E) >> E] = tile[swz_unit(tid + k * T)];
 }
 
 template <typename real, int R>
@@ -462,11 +517,20 @@ __global__ void __launch_bounds__(256, 2)
   for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
   for (int i = tid; i < P.n_gates; i += T) gacc[i] = 0.0;
   const uint64_t base = tile_base(P, blockIdx.x);
-  for (int u = tid; u < nunits; u += T) {
-    const uint64_t g = unit_global(P, base, u, E) >> E;
-    const uint32_t s = swz_unit(u);
-    tp[s] = reinterpret_cast<const U*>(sp)[g];
-    tl[s] = reinterpret_cast<const U*>(sl)[g];
+  {
+    U v[NU], w[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint64_t g = unit_global(P, base, tid + k * T, E) >> E;
+      v[k] = reinterpret_cast<const U*>(sp)[g];
+      w[k] = reinterpret_cast<const U*>(sl)[g];
+    }
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint32_t s = swz_unit(tid + k * T);
+      tp[s] = v[k];
+      tl[s] = w[k];
+    }
   }
   __syncthreads();
   for (int f = 0; f < P.n_phases; ++f) {
@@ -514,9 +578,10 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
   }
-  for (int u = tid; u < nunits; u += T) {
-    const uint64_t g = unit_global(P, base, u, E) >> E;
-    const uint32_t s = swz_unit(u);
+#pragma unroll
+  for (int k = 0; k < NU; ++k) {
+    const uint64_t g = unit_global(P, base, tid + k * T, E) >> E;
+    const uint32_t s = swz_unit(tid + k * T);
     reinterpret_cast<U*>(sp)[g] = tp[s];
     reinterpret_cast<U*>(sl)[g] = tl[s];
   }
@@ -616,7 +681,8 @@ template <typename real>
 __global__ void __launch_bounds__(kMeasThreads)
     probs_kernel(const __grid_constant__ ProbsTable PT, const cpx<real>* __restrict__ psi, int n,
                  double* __restrict__ probs_acc, real* __restrict__ out, int n_real, int64_t circ0) {
-  extern __shared__ float hist[];
+  extern __shared__ __align__(16) unsigned char hist_raw[];
+  real* hist = reinterpret_cast<real*>(hist_raw);
   const int tid = threadIdx.x;
   const int64_t circ = circ0 + blockIdx.y;
   const uint64_t N = 1ull << n;
@@ -637,7 +703,7 @@ __global__ void __launch_bounds__(kMeasThreads)
     const int nb = 1 << d.nbits;
     const bool smem_hist = d.nbits <= 12;
     if (smem_hist) {
-      for (int i = tid; i < nb; i += kMeasThreads) hist[i] = 0.f;
+      for (int i = tid; i < nb; i += kMeasThreads) hist[i] = (real)0;
       __syncthreads();
     }
     double* dst = probs_acc + circ * PT.n_bins + d.acc_off;
@@ -645,13 +711,13 @@ __global__ void __launch_bounds__(kMeasThreads)
       const cpx<real> v = st[w];
       const real p = v.x * v.x + v.y * v.y;
       const uint32_t b = bin_of(d, w);
-      if (smem_hist) atomicAdd(&hist[b], (float)p);
+      if (smem_hist) atomicAdd(&hist[b], p);
       else atomicAdd(&dst[b], (double)p);
     }
     if (smem_hist) {
       __syncthreads();
       for (int i = tid; i < nb; i += kMeasThreads)
-        if (hist[i] != 0.f) atomicAdd(&dst[i], (double)hist[i]);
+        if (hist[i] != (real)0) atomicAdd(&dst[i], (double)hist[i]);
       __syncthreads();
     }
   }
@@ -847,7 +913,7 @@ cudaError_t probs_impl(int n, const ProbsTable& PT, const void* psi, double* pro
   int maxbits = 0;
   for (int i = 0; i < PT.n; ++i)
     if (!PT.p[i].full && PT.p[i].nbits <= 12 && PT.p[i].nbits > maxbits) maxbits = PT.p[i].nbits;
-  const size_t smem = sizeof(float) << maxbits;
+  const size_t smem = sizeof(real) << maxbits;
   auto kern = probs_kernel<real>;
   cudaError_t e = ensure_smem(kern, smem);
   if (e != cudaSuccess) return e;

@@ -35,6 +35,9 @@ enum GateKind : uint8_t {
   GK_D1 = 1,    // diagonal 2x2 on k0 (matrix: 2 entries)
   GK_X = 2,     // controlled bit flip of k0 (no matrix)
   GK_SWAP = 3,  // swap of register bits k0, k1 (no matrix)
+  GK_RXT = 4,   // [[c, -i s], [-i s, c]]: c = M[0].re, s = -M[1].im (4 FMA/amplitude)
+  GK_RYT = 5,   // [[c, -s], [s, c]]:      c = M[0].re, s = -M[1].re
+  GK_PH = 6,    // diag(1, d): only the |1> half is multiplied (d = matrix entry 1)
 };
 
 // Generator kinds of the adjoint gradient: the gradient of a gate

@@ -357,6 +357,22 @@ static uint64_t fill_bits(uint64_t mask, int want, int limit) {
   return mask;
 }
 
+// Register kind of a gate: structured one-factor rotations and phase-type
+// diagonals get cheaper register code than a dense / general diagonal matrix.
+static uint8_t specialised_kind(const HGate& g) {
+  if (g.kind == GK_U1 && g.factors.size() == 1) {
+    if (g.factors[0].op == F_RX) return GK_RXT;
+    if (g.factors[0].op == F_RY) return GK_RYT;
+  }
+  if (g.kind == GK_D1) {
+    bool phase = true;
+    for (const HFactor& f : g.factors)
+      phase &= f.op == F_PHASE || (f.op == F_FIXD && f.m[0].re == 1.0 && f.m[0].im == 0.0);
+    if (phase) return GK_PH;
+  }
+  return g.kind;
+}
+
 // Capacity counters of a pass under construction.
 struct Cap {
   int gates = 0, mats = 0, factors = 0, fixed = 0, grads = 0;
@@ -496,7 +512,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       const HGate& g = gl[idx];
       RGate& r = P.gate[P.n_gates++];
       memset(&r, 0, sizeof(r));
-      r.kind = g.kind;
+      r.kind = specialised_kind(g);
       r.k0 = (uint8_t)regbit_of[pos_of[g.t0]];
       r.k1 = g.t1 >= 0 ? (uint8_t)regbit_of[pos_of[g.t1]] : 0;
       uint32_t cm = 0;
@@ -510,7 +526,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
         r.coef = g.coef;
         P.n_grad++;
       }
-      if (g.kind == GK_U1 || g.kind == GK_D1) {
+      if (g.kind == GK_U1 || g.kind == GK_D1) {  // (also RXT / RYT / PH)
         MatDesc& md = P.mat[P.n_mats];
         r.mat = (uint8_t)P.n_mats++;
         md.diag = g.kind == GK_D1;

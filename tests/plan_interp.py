@@ -12,7 +12,7 @@ lowering and the Pauli expansion of the observables without a GPU.
 import numpy as np
 
 F_FIXED2, F_FIXD, F_RX, F_RY, F_RZ, F_PHASE, F_ROT = range(7)
-GK_U1, GK_D1, GK_X, GK_SWAP = range(4)
+GK_U1, GK_D1, GK_X, GK_SWAP, GK_RXT, GK_RYT, GK_PH = range(7)
 GR_NONE, GR_X, GR_Y, GR_Z, GR_P1 = range(5)
 
 
@@ -67,6 +67,17 @@ def _apply(a, r, M):
         for tgt, c in ((r["k1"], cm | b0), (k0, cm | b1), (r["k1"], cm | b0)):
             _apply(a, {"kind": GK_X, "k0": tgt, "cmask": c}, None)
         return
+    if kind == GK_RXT:
+        c, sn = M[0, 0].real, -M[0, 1].imag
+        M = np.array([[c, -1j * sn], [-1j * sn, c]])
+        kind = GK_U1
+    elif kind == GK_RYT:
+        c, sn = M[0, 0].real, -M[0, 1].real
+        M = np.array([[c, -sn], [sn, c]], dtype=complex)
+        kind = GK_U1
+    elif kind == GK_PH:
+        M = np.diag([1.0, M[1, 1]])
+        kind = GK_D1
     for i in range(NR):
         if kind == GK_D1:
             if (i & cm) == cm:
@@ -172,7 +183,7 @@ def run_pass(P, psi, prm, lam=None, grads=None):
             a = tp[addr]
             l = tl[addr] if tl is not None else None
             for r in ph["gates"]:
-                M = mats[r["mat"]] if r["kind"] in (GK_U1, GK_D1) else None
+                M = mats[r["mat"]] if r["kind"] not in (GK_X, GK_SWAP) else None
                 if l is not None and r["grad"] != GR_NONE:
                     grads[r["slot"]] += _grad(a, l, r)
                 _apply(a, r, M)
