@@ -167,6 +167,18 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
                  void* out_real, const void* init, void* workspace, size_t workspace_bytes,
                  void* stream);
 
+/* ---- forward without allocation -----------------------------------------
+ * No counterpart in the reference.  Same as tedq_run, but the workspace is a
+ * 1 MiB static device array of this library instead of a caller buffer, for
+ * callers that cannot allocate device memory where they run circuits (inside
+ * stream capture, allocator callbacks, real-time loops, embedders whose device
+ * memory belongs to another runtime).  Batches needing more than 1 MiB of
+ * workspace are rejected (TEDQ_ERR_ARG).  The first call on a device looks up
+ * the array's address and should come before any stream capture; calls that
+ * overlap on the GPU share the array and race. */
+int32_t tedq_run_noalloc(tedq_program_t* prog, const void* params, int64_t batch, void* psi,
+                         void* out_real, const void* init, void* stream);
+
 /* ---- adjoint backward ----------------------------------------------------
  * Vector-Jacobian product of tedq_run: grad[b][s] = d/dparam[b][s] of
  *   sum_k dy_real[b][k] * out_real[b][k] + Re sum_x conj(dy_state[b][x]) psi[b][x]

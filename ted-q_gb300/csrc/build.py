@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(PKG_ROOT, "_build")
 OUT = os.path.join(PKG_ROOT, "tedq_gb300", "libtedq_gb300.so")
 
-CU_SOURCES = ["sv_kernels.cu"]
+CU_SOURCES = ["sv_kernels.cu", "noalloc.cu"]
 CPP_SOURCES = ["sv_program.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

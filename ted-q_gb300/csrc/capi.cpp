@@ -341,3 +341,7 @@ int32_t tedq_profile_read(tedq_program_t* prog, tedq_profile_t* out) {
 }
 
 }  // extern "C"
+
+// Records an error message for tedq_last_error from other translation units
+// of this library (C++ linkage, not part of the public ABI).
+int32_t tedq_record_error(int32_t status, const char* msg) { return fail(status, msg ? msg : ""); }

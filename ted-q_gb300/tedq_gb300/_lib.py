@@ -75,6 +75,7 @@ SIGNATURES = {
                            c_void_p]),
     "tedq_run_adjoint": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tedq_run_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tedq_profile_enable": (c_int32, [c_void_p, c_int32]),
     "tedq_profile_read": (c_int32, [c_void_p, POINTER(Profile)]),
 }
