@@ -1,0 +1,653 @@
+// sv_device.cuh -- device code of the state-vector passes, shared by the
+// generic pass kernels (sv_kernels.cu) and by the per-circuit kernels that
+// sv_jit.cpp generates and compiles with NVRTC at program-creation time.
+//
+// A pass kernel is written as
+//     FwdPass<real, R> c(...);          // matrices + tile staging
+//     c.begin(f); <gates on c.a>; c.end(f);   // one register phase
+//     c.finish();                       // tile back to HBM
+// In the generic kernels the gates of a phase are dispatched at run time; in
+// the generated kernels every gate is a template instance with its register
+// bit and control mask as compile-time constants, so control tests fold away
+// and bit flips become register renames.
+//
+// Self-contained: compiles under nvcc and NVRTC (no host headers).
+#pragma once
+#include "sv_plan.h"
+
+namespace tedq {
+namespace dev {
+
+template <typename real>
+struct alignas(2 * sizeof(real)) cpx {
+  real x, y;
+};
+
+template <typename real>
+struct Unit;
+template <>
+struct alignas(16) Unit<float> {
+  cpx<float> v[2];
+};
+template <>
+struct alignas(16) Unit<double> {
+  cpx<double> v[1];
+};
+
+template <typename real>
+struct UnitsPerAmp;
+template <>
+struct UnitsPerAmp<float> {
+  static constexpr int E = 1;  // log2 amplitudes per 16-byte unit
+};
+template <>
+struct UnitsPerAmp<double> {
+  static constexpr int E = 0;
+};
+
+// Compile-time control mask (generated kernels) -- converts to unsigned so the
+// same gate templates accept a run-time mask (generic kernels).
+template <unsigned V>
+struct CM {
+  __device__ __forceinline__ constexpr operator unsigned() const { return V; }
+};
+
+template <typename real>
+__device__ __forceinline__ cpx<real> mk(real x, real y) {
+  cpx<real> r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+template <typename real>
+__device__ __forceinline__ cpx<real> cmul(cpx<real> a, cpx<real> b) {
+  return mk<real>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// m0 * x0 + m1 * x1
+template <typename real>
+__device__ __forceinline__ cpx<real> cmac2(cpx<real> m0, cpx<real> x0, cpx<real> m1, cpx<real> x1) {
+  real re = m0.x * x0.x;
+  re = fma(-m0.y, x0.y, re);
+  re = fma(m1.x, x1.x, re);
+  re = fma(-m1.y, x1.y, re);
+  real im = m0.x * x0.y;
+  im = fma(m0.y, x0.x, im);
+  im = fma(m1.x, x1.y, im);
+  im = fma(m1.y, x1.x, im);
+  return mk<real>(re, im);
+}
+template <typename real>
+__device__ __forceinline__ cpx<real> cconj(cpx<real> a) {
+  return mk<real>(a.x, -a.y);
+}
+// Im(conj(a) b), Re(conj(a) b)
+template <typename real>
+__device__ __forceinline__ real imcb(cpx<real> a, cpx<real> b) {
+  return a.x * b.y - a.y * b.x;
+}
+template <typename real>
+__device__ __forceinline__ real recb(cpx<real> a, cpx<real> b) {
+  return a.x * b.x + a.y * b.y;
+}
+
+__device__ __forceinline__ void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
+
+template <typename real>
+__device__ __forceinline__ real pval(const Factor& F, int j, const real* prm) {
+  return F.slot[j] >= 0 ? prm[F.slot[j]] : (real)F.val[j];
+}
+
+template <typename real>
+__device__ __forceinline__ cpx<real> fixed_at(const PassParams& P, int i) {
+  return mk<real>((real)P.fixed[i].re, (real)P.fixed[i].im);
+}
+
+// One factor as a dense 2x2 (row-major).  Gate definitions follow the
+// reference (tedq/QInterpreter/operators/qubit.py: RX :990-997, RY :1048-1055,
+// RZ :1106-1112, PhaseShift :1253-1257, Rot :1169-1189).
+template <typename real>
+__device__ void factor_mat(const PassParams& P, const Factor& F, const real* prm, cpx<real>* m) {
+  const real zero = 0, one = 1;
+  switch (F.op) {
+    case F_FIXED2:
+      for (int k = 0; k < 4; ++k) m[k] = fixed_at<real>(P, F.fix + k);
+      break;
+    case F_FIXD:
+      m[0] = fixed_at<real>(P, F.fix);
+      m[1] = m[2] = mk<real>(zero, zero);
+      m[3] = fixed_at<real>(P, F.fix + 1);
+      break;
+    case F_RX: {
+      real s, c;
+      sincos_(pval<real>(F, 0, prm) / (real)2, &s, &c);
+      m[0] = m[3] = mk<real>(c, zero);
+      m[1] = m[2] = mk<real>(zero, -s);
+      break;
+    }
+    case F_RY: {
+      real s, c;
+      sincos_(pval<real>(F, 0, prm) / (real)2, &s, &c);
+      m[0] = m[3] = mk<real>(c, zero);
+      m[1] = mk<real>(-s, zero);
+      m[2] = mk<real>(s, zero);
+      break;
+    }
+    case F_RZ: {
+      real s, c;
+      sincos_(pval<real>(F, 0, prm) / (real)2, &s, &c);
+      m[0] = mk<real>(c, -s);
+      m[3] = mk<real>(c, s);
+      m[1] = m[2] = mk<real>(zero, zero);
+      break;
+    }
+    case F_PHASE: {
+      real s, c;
+      sincos_(pval<real>(F, 0, prm), &s, &c);
+      m[0] = mk<real>(one, zero);
+      m[3] = mk<real>(c, s);
+      m[1] = m[2] = mk<real>(zero, zero);
+      break;
+    }
+    default: {  // F_ROT
+      real phi = pval<real>(F, 0, prm), th = pval<real>(F, 1, prm), om = pval<real>(F, 2, prm);
+      real s, c, sp, cp, sm, cm;
+      sincos_(th / (real)2, &s, &c);
+      sincos_((phi + om) / (real)2, &sp, &cp);
+      sincos_((phi - om) / (real)2, &sm, &cm);
+      m[0] = mk<real>(cp * c, -sp * c);
+      m[1] = mk<real>(-cm * s, -sm * s);
+      m[2] = mk<real>(cm * s, -sm * s);
+      m[3] = mk<real>(cp * c, sp * c);
+      break;
+    }
+  }
+}
+
+// Matrix i of a pass: product of its factors (first factor applied first),
+// conjugate-transposed for the adjoint sweep.  Diagonal matrices keep 2 entries.
+template <typename real>
+__device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<real>* out) {
+  const MatDesc md = P.mat[i];
+  cpx<real> M[4], F[4], T[4];
+  factor_mat<real>(P, P.factor[md.f0], prm, M);
+  for (int j = 1; j < md.nf; ++j) {
+    factor_mat<real>(P, P.factor[md.f0 + j], prm, F);
+    T[0] = cmac2(F[0], M[0], F[1], M[2]);
+    T[1] = cmac2(F[0], M[1], F[1], M[3]);
+    T[2] = cmac2(F[2], M[0], F[3], M[2]);
+    T[3] = cmac2(F[2], M[1], F[3], M[3]);
+    M[0] = T[0];
+    M[1] = T[1];
+    M[2] = T[2];
+    M[3] = T[3];
+  }
+  if (md.dagger) {
+    cpx<real> t = M[1];
+    M[1] = cconj(M[2]);
+    M[2] = cconj(t);
+    M[0] = cconj(M[0]);
+    M[3] = cconj(M[3]);
+  }
+  if (md.diag) {
+    out[0] = M[0];
+    out[1] = M[3];
+  } else {
+    for (int k = 0; k < 4; ++k) out[k] = M[k];
+  }
+}
+
+// ---------------------------------------------------------------- register gates
+// a[2^R]: the thread's amplitudes; bit k of the register index is register
+// bit k.  Ctl is an unsigned run-time mask or a CM<> constant.
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_u1(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+  const cpx<real> m0 = M[0], m1 = M[1], m2 = M[2], m3 = M[3];
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = cmac2(m0, x0, m1, x1);
+    a[j] = cmac2(m2, x0, m3, x1);
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_d1(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+  const cpx<real> d0 = M[0], d1 = M[1];
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    a[i] = cmul((i >> K) & 1 ? d1 : d0, a[i]);
+  }
+}
+
+// RX-type [[c, -i s], [-i s, c]] (RX, or RX^dagger with s negated)
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_rxt(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+  const real c = M[0].x, sn = -M[1].y;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = mk<real>(fma(c, x0.x, sn * x1.y), fma(c, x0.y, -sn * x1.x));
+    a[j] = mk<real>(fma(c, x1.x, sn * x0.y), fma(c, x1.y, -sn * x0.x));
+  }
+}
+
+// RY-type [[c, -s], [s, c]]
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ryt(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+  const real c = M[0].x, sn = -M[1].x;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = mk<real>(fma(c, x0.x, -sn * x1.x), fma(c, x0.y, -sn * x1.y));
+    a[j] = mk<real>(fma(sn, x0.x, c * x1.x), fma(sn, x0.y, c * x1.y));
+  }
+}
+
+// diag(1, d): multiply the |1> half only
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ph(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+  const cpx<real> d = M[1];
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (!(i & (1 << K))) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    a[i] = cmul(d, a[i]);
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_x(cpx<real>* a, Ctl cm) {
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> t = a[i];
+    a[i] = a[j];
+    a[j] = t;
+  }
+}
+
+// Per-thread part of Im <lambda| G |psi> on the control subspace
+// (G = X, Y, Z or P1 = |1><1| on register bit K).
+template <int G, int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ real grad_part(const cpx<real>* p, const cpx<real>* l, Ctl cm) {
+  real acc = 0;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    if (G == GR_X) acc += imcb(l[i], p[j]) + imcb(l[j], p[i]);
+    if (G == GR_Y) acc += recb(l[j], p[i]) - recb(l[i], p[j]);
+    if (G == GR_Z) acc += imcb(l[i], p[i]) - imcb(l[j], p[j]);
+    if (G == GR_P1) acc += imcb(l[j], p[j]);
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------- run-time dispatch
+
+template <int R, typename real, int K = 0>
+__device__ __forceinline__ void dispatch_gate(int kind, int k, cpx<real>* a, const cpx<real>* M, unsigned cm) {
+  if constexpr (K < R) {
+    if (k == K) {
+      switch (kind) {
+        case GK_U1: apply_u1<K, R, real>(a, M, cm); break;
+        case GK_D1: apply_d1<K, R, real>(a, M, cm); break;
+        case GK_RXT: apply_rxt<K, R, real>(a, M, cm); break;
+        case GK_RYT: apply_ryt<K, R, real>(a, M, cm); break;
+        case GK_PH: apply_ph<K, R, real>(a, M, cm); break;
+        default: apply_x<K, R, real>(a, cm); break;
+      }
+    } else {
+      dispatch_gate<R, real, K + 1>(kind, k, a, M, cm);
+    }
+  }
+}
+
+template <int R, typename real>
+__device__ __forceinline__ void apply_rgate(const RGate& r, cpx<real>* a, const cpx<real>* M) {
+  if (r.kind == GK_SWAP) {
+    const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
+    dispatch_gate<R, real>(GK_X, r.k1, a, M, r.cmask | b0);
+    dispatch_gate<R, real>(GK_X, r.k0, a, M, r.cmask | b1);
+    dispatch_gate<R, real>(GK_X, r.k1, a, M, r.cmask | b0);
+  } else {
+    dispatch_gate<R, real>(r.kind, r.k0, a, M, r.cmask);
+  }
+}
+
+template <int R, typename real, int K = 0>
+__device__ __forceinline__ real dispatch_grad(int g, int k, const cpx<real>* p, const cpx<real>* l, unsigned cm) {
+  if constexpr (K < R) {
+    if (k == K) {
+      switch (g) {
+        case GR_X: return grad_part<GR_X, K, R, real>(p, l, cm);
+        case GR_Y: return grad_part<GR_Y, K, R, real>(p, l, cm);
+        case GR_Z: return grad_part<GR_Z, K, R, real>(p, l, cm);
+        default: return grad_part<GR_P1, K, R, real>(p, l, cm);
+      }
+    }
+    return dispatch_grad<R, real, K + 1>(g, k, p, l, cm);
+  }
+  return (real)0;
+}
+
+// ---------------------------------------------------------------- tile staging
+
+__device__ __forceinline__ uint64_t tile_base(const PassParams& P, uint32_t tile) {
+  uint64_t base = 0;
+  for (int k = 0; k < P.n_outer; ++k)
+    if ((tile >> k) & 1) base |= 1ull << P.outer[k];
+  return base;
+}
+
+template <typename real>
+__device__ __forceinline__ Unit<real> load_unit(const PassParams& P, const cpx<real>* st, uint64_t g,
+                                                const cpx<real>* init) {
+  constexpr int E = UnitsPerAmp<real>::E;
+  Unit<real> v;
+  if (P.init == 0) {
+    v = reinterpret_cast<const Unit<real>*>(st)[g >> E];
+  } else {
+#pragma unroll
+    for (int k = 0; k < (1 << E); ++k) {
+      const uint64_t q = g + k;
+      cpx<real> a = mk<real>((real)0, (real)0);
+      if (P.init == 1) {
+        if (q == 0) a.x = (real)1;
+      } else if ((q & ((1ull << P.pad_bits) - 1)) == 0) {
+        a = init[q >> P.pad_bits];
+      }
+      v.v[k] = a;
+    }
+  }
+  return v;
+}
+
+// Dense fixed k-qubit matrix applied directly on the shared-memory tile.
+template <typename real>
+__device__ void dense_phase(const PassParams& P, const Phase& ph, Unit<real>* tile, int tid, int T) {
+  constexpr int E = UnitsPerAmp<real>::E;
+  cpx<real>* amp = reinterpret_cast<cpx<real>*>(tile);
+  const int k = ph.dk, d = 1 << k;
+  uint32_t dmask = 0;
+  for (int i = 0; i < k; ++i) dmask |= 1u << ph.dpos[i];
+  const int ngroups = 1 << (P.m - k);
+  for (int grp = tid; grp < ngroups; grp += T) {
+    uint32_t base = 0, rem = grp;
+    for (int p = 0; p < P.m; ++p)
+      if (!((dmask >> p) & 1)) {
+        if (rem & 1) base |= 1u << p;
+        rem >>= 1;
+      }
+    if ((base & ph.dcmask) != ph.dcmask) continue;
+    cpx<real> v[8], w[8];
+    uint32_t addr[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      if (r < d) {
+        uint32_t t = base;
+        for (int i = 0; i < k; ++i)
+          if ((r >> (k - 1 - i)) & 1) t |= 1u << ph.dpos[i];
+        addr[r] = (swz_unit(t >> E) << E) | (t & ((1u << E) - 1));
+        v[r] = amp[addr[r]];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      if (r < d) {
+        cpx<real> acc = mk<real>((real)0, (real)0);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          if (c < d) {
+            cpx<real> m = ph.dagger ? cconj(fixed_at<real>(P, ph.dfix + c * d + r))
+                                    : fixed_at<real>(P, ph.dfix + r * d + c);
+            cpx<real> t = cmul(m, v[c]);
+            acc.x += t.x;
+            acc.y += t.y;
+          }
+        }
+        w[r] = acc;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+      if (r < d) amp[addr[r]] = w[r];
+  }
+}
+
+// Thread part of the staging addresses: thread-index bits map to fixed
+// global-offset and shared-memory-unit contributions (tables of the pass).
+__device__ __forceinline__ void thread_offsets(const PassParams& P, int tid, int ntid, uint64_t& g, uint32_t& s) {
+  for (int b = 0; b < ntid; ++b)
+    if ((tid >> b) & 1) {
+      g |= P.gtid[b];
+      s ^= P.stid[b];
+    }
+}
+
+// ---------------------------------------------------------------- forward pass
+
+template <typename real, int R>
+struct FwdPass {
+  using C = cpx<real>;
+  using U = Unit<real>;
+  static constexpr int E = UnitsPerAmp<real>::E;
+  static constexpr int NR = 1 << R;
+  static constexpr int NU = NR >> E;
+  const PassParams& P;
+  U* tile;
+  C (*mats)[4];
+  C* st;
+  int tid;
+  uint64_t gthr;
+  uint32_t sthr;
+  uint32_t bu;
+  C a[NR];
+
+  __device__ __forceinline__ FwdPass(const PassParams& P_, U* tile_, C (*mats_)[4], C* psi, const real* params,
+                                     int n_params, const C* init, int64_t circ0)
+      : P(P_), tile(tile_), mats(mats_) {
+    tid = threadIdx.x;
+    const int T = blockDim.x;
+    const int64_t circ = circ0 + blockIdx.y;
+    st = psi + (circ << P.n);
+    const real* prm = params ? params + circ * n_params : nullptr;
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
+    gthr = tile_base(P, blockIdx.x);
+    sthr = 0;
+    thread_offsets(P, tid, P.m - R, gthr, sthr);
+    U v[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
+#pragma unroll
+    for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = v[k];
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void begin(int f) {
+    const Phase& ph = P.phase[f];
+    bu = 0;
+    for (int b = 0; b < ph.ntid; ++b)
+      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      const U v = tile[bu ^ ph.reg_off[j]];
+#pragma unroll
+      for (int k = 0; k < (1 << E); ++k) a[(j << E) + k] = v.v[k];
+    }
+  }
+
+  __device__ __forceinline__ void end(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      U v;
+#pragma unroll
+      for (int k = 0; k < (1 << E); ++k) v.v[k] = a[(j << E) + k];
+      tile[bu ^ ph.reg_off[j]] = v;
+    }
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void dense(int f) {
+    dense_phase<real>(P, P.phase[f], tile, tid, blockDim.x);
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void finish() {
+    U* gst = reinterpret_cast<U*>(st);
+#pragma unroll
+    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = tile[sthr ^ P.sk[k]];
+  }
+};
+
+// ---------------------------------------------------------------- adjoint pass
+
+template <typename real, int R>
+struct BwdPass {
+  using C = cpx<real>;
+  using U = Unit<real>;
+  static constexpr int E = UnitsPerAmp<real>::E;
+  static constexpr int NR = 1 << R;
+  static constexpr int NU = NR >> E;
+  const PassParams& P;
+  U* tp;
+  U* tl;
+  C (*mats)[4];
+  double* gacc;
+  C* sp;
+  C* sl;
+  double* grad_acc;
+  int64_t circ;
+  int n_params;
+  int tid;
+  uint64_t gthr;
+  uint32_t sthr;
+  uint32_t bu;
+  C a[NR];
+  C l[NR];
+
+  __device__ __forceinline__ BwdPass(const PassParams& P_, U* smem, C (*mats_)[4], double* gacc_, C* psi, C* lam,
+                                     const real* params, int n_params_, double* grad_acc_, int64_t circ0)
+      : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_) {
+    tid = threadIdx.x;
+    const int T = blockDim.x;
+    tp = smem;
+    tl = smem + (1 << (P.m - E));
+    circ = circ0 + blockIdx.y;
+    sp = psi + (circ << P.n);
+    sl = lam + (circ << P.n);
+    const real* prm = params ? params + circ * n_params : nullptr;
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
+    for (int i = tid; i < P.n_gates; i += T) gacc[i] = 0.0;
+    gthr = tile_base(P, blockIdx.x);
+    sthr = 0;
+    thread_offsets(P, tid, P.m - R, gthr, sthr);
+    U v[NU], w[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint64_t g = (gthr | P.gk[k]) >> E;
+      v[k] = reinterpret_cast<const U*>(sp)[g];
+      w[k] = reinterpret_cast<const U*>(sl)[g];
+    }
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      tp[sthr ^ P.sk[k]] = v[k];
+      tl[sthr ^ P.sk[k]] = w[k];
+    }
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void begin(int f) {
+    const Phase& ph = P.phase[f];
+    bu = 0;
+    for (int b = 0; b < ph.ntid; ++b)
+      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      const U v = tp[bu ^ ph.reg_off[j]];
+      const U w = tl[bu ^ ph.reg_off[j]];
+#pragma unroll
+      for (int k = 0; k < (1 << E); ++k) {
+        a[(j << E) + k] = v.v[k];
+        l[(j << E) + k] = w.v[k];
+      }
+    }
+  }
+
+  __device__ __forceinline__ void end(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      U v, w;
+#pragma unroll
+      for (int k = 0; k < (1 << E); ++k) {
+        v.v[k] = a[(j << E) + k];
+        w.v[k] = l[(j << E) + k];
+      }
+      tp[bu ^ ph.reg_off[j]] = v;
+      tl[bu ^ ph.reg_off[j]] = w;
+    }
+    __syncthreads();
+  }
+
+  // Warp-reduce one gate's partial gradient and add it to the CTA accumulator.
+  __device__ __forceinline__ void grad(int g, real part, float coef) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((tid & 31) == 0) atomicAdd(&gacc[g], (double)part * (double)coef);
+  }
+
+  __device__ __forceinline__ void dense(int f) {
+    dense_phase<real>(P, P.phase[f], tp, tid, blockDim.x);
+    dense_phase<real>(P, P.phase[f], tl, tid, blockDim.x);
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void finish() {
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint64_t g = (gthr | P.gk[k]) >> E;
+      reinterpret_cast<U*>(sp)[g] = tp[sthr ^ P.sk[k]];
+      reinterpret_cast<U*>(sl)[g] = tl[sthr ^ P.sk[k]];
+    }
+    if (P.n_grad) {
+      for (int g = tid; g < P.n_gates; g += blockDim.x) {
+        const int32_t slot = P.gate[g].slot;
+        if (slot >= 0) atomicAdd(&grad_acc[circ * n_params + slot], gacc[g]);
+      }
+    }
+  }
+};
+
+}  // namespace dev
+}  // namespace tedq
+
+// Kernel prologues shared by the generic and the generated pass kernels.
+#define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                  \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
+  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::Unit<REAL>*>(tedq_smem_raw), tedq_mats, \
+                                 psi, params, n_params, init, circ0);
+
+#define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                  \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
+  __shared__ double tedq_gacc[tedq::kMaxPassGates];                                                  \
+  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::Unit<REAL>*>(tedq_smem_raw), tedq_mats, \
+                                 tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);

@@ -15,7 +15,17 @@
 // Everything a kernel needs about one pass travels in one PassParams struct
 // passed by value (``__grid_constant__``); the program needs no device memory.
 #pragma once
+#if defined(__CUDACC_RTC__)
+typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
+typedef short int16_t;
+typedef int int32_t;
+typedef long long int64_t;
+#else
 #include <stdint.h>
+#endif
 
 namespace tedq {
 
@@ -119,6 +129,13 @@ struct PassParams {
   uint8_t pad[2];
   uint8_t hi[kMaxTileBits];      // global bit of tile bit c+i
   uint8_t outer[kMaxStateBits];  // global bit of outer-index bit i
+  // Tile staging: thread tid stages units u = tid + k * 2^(m-R), k < 2^(R-e).
+  // Global amplitude offset = tile base | OR of gtid[b] over set bits b of
+  // tid | gk[k]; shared-memory unit = XOR of stid[b] ^ sk[k] (swizzled).
+  uint64_t gtid[kMaxTidBits];
+  uint64_t gk[kMaxRegUnits];
+  uint32_t stid[kMaxTidBits];
+  uint32_t sk[kMaxRegUnits];
   Phase phase[kMaxPhases];
   RGate gate[kMaxPassGates];
   MatDesc mat[kMaxMats];

@@ -421,6 +421,21 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
     for (int b = 0; b < ns; ++b)
       if (!(L >> b & 1)) P.outer[j++] = (uint8_t)b;
   }
+  // staging tables: unit bit b is tile bit b + e, i.e. global bit tb[b + e]
+  {
+    const int ntid = G.m - G.R, nk = 1 << (G.R - G.e);
+    for (int b = 0; b < ntid; ++b) {
+      P.gtid[b] = 1ull << tb[b + G.e];
+      P.stid[b] = swz_unit(1u << b);
+    }
+    for (int k = 0; k < nk; ++k) {
+      uint64_t g = 0;
+      for (int j = 0; (k >> j) != 0; ++j)
+        if ((k >> j) & 1) g |= 1ull << tb[ntid + j + G.e];
+      P.gk[k] = g;
+      P.sk[k] = swz_unit((uint32_t)k << ntid);
+    }
+  }
   int nfixed = 0;
   auto push_fixed = [&](const CD* v, int cnt) {
     int at = nfixed;
@@ -783,6 +798,14 @@ std::string describe_schedule(const Program& p, bool adjoint) {
     for (int j = 0; j < P.m - P.c; ++j) o << (j ? "," : "") << (int)P.hi[j];
     o << "],\"outer\":[";
     for (int j = 0; j < P.n_outer; ++j) o << (j ? "," : "") << (int)P.outer[j];
+    o << "],\"gtid\":[";
+    for (int j = 0; j < P.m - P.R; ++j) o << (j ? "," : "") << P.gtid[j];
+    o << "],\"stid\":[";
+    for (int j = 0; j < P.m - P.R; ++j) o << (j ? "," : "") << P.stid[j];
+    o << "],\"gk\":[";
+    for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << P.gk[j];
+    o << "],\"sk\":[";
+    for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << P.sk[j];
     o << "],\"phases\":[";
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];

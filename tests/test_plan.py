@@ -127,3 +127,24 @@ def test_plan_multi_pass_against_oracle(n, tile):
     g = plan_interp.adjoint(cc.describe(adjoint=True), prm, psi.copy(), dy)
     _, want_g = oracle.value_and_grad(spec, prm, dy, torch.complex128)
     np.testing.assert_allclose(g, want_g.numpy(), atol=1e-11)
+
+
+@pytest.mark.parametrize("n,adjoint", [(12, False), (16, False), (16, True), (20, True)])
+def test_staging_tables_match_tile_map(n, adjoint):
+    """gtid/gk/stid/sk reproduce the tile gather and the swizzle for every unit."""
+    spec = _hea_spec(n, 2, seed=1)
+    desc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300").describe(adjoint=adjoint)
+    for P in desc["passes"]:
+        m, e, R = P["m"], P["e"], P["R"]
+        T, NU = 1 << (m - R), 1 << (R - e)
+        g_direct = plan_interp._tile_index(P, 0)
+        for tid in range(T):
+            g_t, s_t = 0, 0
+            for b in range(m - R):
+                if (tid >> b) & 1:
+                    g_t |= P["gtid"][b]
+                    s_t ^= P["stid"][b]
+            for k in range(NU):
+                u = tid + k * T
+                assert (g_t | P["gk"][k]) == g_direct[u << e]
+                assert (s_t ^ P["sk"][k]) == plan_interp.swz_unit(u)
