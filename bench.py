@@ -273,7 +273,10 @@ def run_ours(a):
     from tedq_gb300 import _lib
 
     spec = vqc_spec(a.qubits, a.layers)
-    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain)
+    t_compile = time.perf_counter()
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain, jit=a.jit)
+    jit_reason = cc._prog.jit_wait()
+    t_compile = time.perf_counter() - t_compile
     info = cc.program_info
     P = cc.num_params
     B = a.batch
@@ -374,6 +377,8 @@ def run_ours(a):
                                     "measure": prof.meas_ms / a.steps, "lambda_etc": prof.lam_ms / a.steps},
             "schedule": {k: info[k] for k in ("n_fwd_passes", "n_bwd_passes", "n_fwd_phases", "n_bwd_phases",
                                               "n_fused_gates", "n_elem_gates")},
+            "pass_kernels": "generic" if jit_reason else "specialised (NVRTC, sm_103a)",
+            "compile_s": round(t_compile, 3),
             "clocks": clk}
     if not a.no_plain:
         try:
@@ -403,6 +408,7 @@ def main():
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
+    ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)

@@ -107,7 +107,10 @@ typedef struct tedq_options {
                           or TEDQ_PREC_C128 (complex128 state, float64)            */
   int32_t fuse;        /* 1: fused multi-gate passes; 0: one pass per gate (plain) */
   int32_t tile_qubits; /* 0 = default tile size (2^13 amplitudes for c64)          */
-  int32_t reserved[5];
+  int32_t jit;         /* specialised per-circuit pass kernels compiled with NVRTC:
+                          0 = auto (on for states of >= 14 qubits), 1 = on, -1 = off;
+                          the environment variable TEDQ_GB300_JIT=0 turns it off   */
+  int32_t reserved[4];
 } tedq_options_t;
 
 typedef struct tedq_program tedq_program_t;
@@ -127,7 +130,9 @@ typedef struct tedq_program_info {
   int32_t n_elem_gates;      /* elementary gates (adjoint)                         */
   int32_t precision;
   int64_t workspace_per_circuit; /* bytes of workspace per circuit of a batch      */
-  int64_t reserved[4];
+  int32_t jit_state;         /* 0 off, 1 compiling, 2 compiled, 3 loaded, -1 failed  */
+  int32_t pad;
+  int64_t reserved[3];
 } tedq_program_info_t;
 
 /* ---- library ------------------------------------------------------------ */
@@ -146,6 +151,11 @@ int32_t tedq_program_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
                             const tedq_options_t* opts, tedq_program_t** out);
 int32_t tedq_program_destroy(tedq_program_t* prog);
 int32_t tedq_program_info(const tedq_program_t* prog, tedq_program_info_t* info);
+/* Waits for the program's specialised kernels to be compiled (host only, no
+ * GPU needed).  TEDQ_OK when they are ready, TEDQ_ERR_UNSUPPORTED when they are
+ * off or could not be built (reason in tedq_last_error); the generic pass
+ * kernels are used then. */
+int32_t tedq_program_jit_wait(tedq_program_t* prog);
 /* Device workspace (bytes) that tedq_run / tedq_run_adjoint need for a batch. */
 int64_t tedq_program_workspace_bytes(const tedq_program_t* prog, int64_t batch);
 /* Schedule export for inspection: writes a JSON description of the passes

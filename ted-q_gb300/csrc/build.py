@@ -23,7 +23,9 @@ BUILD = os.path.join(PKG_ROOT, "_build")
 OUT = os.path.join(PKG_ROOT, "tedq_gb300", "libtedq_gb300.so")
 
 CU_SOURCES = ["sv_kernels.cu", "noalloc.cu"]
-CPP_SOURCES = ["sv_program.cpp", "capi.cpp"]
+CPP_SOURCES = ["sv_program.cpp", "capi.cpp", "sv_jit.cpp"]
+# headers compiled again at run time by NVRTC for the per-circuit kernels
+JIT_HEADERS = ["sv_plan.h", "sv_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -46,11 +48,30 @@ def run(cmd, verbose):
     return r.stdout + r.stderr
 
 
+def write_jit_headers():
+    """Embed the device headers as C string literals (_build/jit_headers.inc)."""
+    names, srcs = [], []
+    for h in JIT_HEADERS:
+        with open(os.path.join(HERE, h)) as f:
+            text = f.read()
+        assert ')tedqjit"' not in text
+        names.append('"%s"' % h)
+        srcs.append('R"tedqjit(' + text + ')tedqjit"')
+    out = ("static const char* const kJitHeaderNames[%d] = {%s};\n" % (len(names), ", ".join(names)) +
+           "static const char* const kJitHeaderSrc[%d] = {\n%s};\n" % (len(srcs), ",\n".join(srcs)))
+    path = os.path.join(BUILD, "jit_headers.inc")
+    old = open(path).read() if os.path.exists(path) else None
+    if old != out:
+        with open(path, "w") as f:
+            f.write(out)
+
+
 def build(jobs=4, verbose=False, ptxas_verbose=False):
     cuda = cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
-    common_inc = ["-I", INCLUDE, "-I", HERE]
+    write_jit_headers()
+    common_inc = ["-I", INCLUDE, "-I", HERE, "-I", BUILD]
     cmds, objs = [], []
     for src in CU_SOURCES:
         obj = os.path.join(BUILD, src + ".o")

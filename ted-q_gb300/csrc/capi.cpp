@@ -7,12 +7,18 @@
 // synchronisation.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <future>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "sv_jit.h"
 #include "sv_kernels.cuh"
 #include "sv_program.h"
 #include "tedq_gb300.h"
@@ -32,6 +38,17 @@ struct tedq_program {
   ProbsTable probs;
   bool profiling = false;
   std::vector<ProfEvent> events;
+  // specialised kernels: compiled in the background from program creation,
+  // loaded per device on first use
+  bool jit_on = false;
+  int jit_state = 0;  // 0 off, 1 compiling, 2 compiled, 3 loaded, -1 failed
+  std::future<std::tuple<bool, std::vector<std::string>, std::string>> jit_future;
+  std::vector<JitSource> jit_srcs;
+  std::vector<std::string> jit_cubins;
+  std::string jit_err;
+  std::mutex jit_mu;
+  JitKernels jit_dev[64];
+  bool jit_tried[64] = {false};
 };
 
 namespace {
@@ -61,6 +78,46 @@ cudaError_t timed(tedq_program* h, int family, int64_t amp_passes, cudaStream_t 
   cudaEventRecord(ev.b, s);
   h->events.push_back(ev);
   return e;
+}
+
+// Waits for the background compile; returns true when a cubin is available.
+bool jit_compiled(tedq_program* h) {
+  if (!h->jit_on) return false;
+  if (h->jit_state == 1) {
+    auto r = h->jit_future.get();
+    if (std::get<0>(r)) {
+      h->jit_cubins = std::move(std::get<1>(r));
+      h->jit_state = 2;
+    } else {
+      h->jit_err = std::get<2>(r);
+      h->jit_state = -1;
+      fprintf(stderr, "tedq_gb300: specialised kernels unavailable, using generic kernels: %s\n",
+              h->jit_err.substr(0, 300).c_str());
+    }
+  }
+  return h->jit_state >= 2;
+}
+
+// The specialised kernels of the current device, or nullptr (generic kernels).
+JitKernels* jit_kernels(tedq_program* h) {
+  if (!h->jit_on) return nullptr;
+  std::lock_guard<std::mutex> lock(h->jit_mu);
+  if (!jit_compiled(h)) return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!h->jit_tried[dev]) {
+    h->jit_tried[dev] = true;
+    std::string err;
+    if (jit_load(h->jit_cubins, h->jit_srcs, (int)h->p->fwd.passes.size(), (int)h->p->bwd.passes.size(),
+                 h->jit_dev[dev], err)) {
+      h->jit_state = 3;
+    } else {
+      h->jit_dev[dev] = JitKernels();
+      fprintf(stderr, "tedq_gb300: loading specialised kernels failed, using generic kernels: %s\n", err.c_str());
+    }
+  }
+  JitKernels& k = h->jit_dev[dev];
+  return k.modules.empty() ? nullptr : &k;
 }
 
 int64_t align256(int64_t v) { return (v + 255) & ~int64_t(255); }
@@ -144,6 +201,21 @@ int32_t tedq_program_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
     h = new tedq_program();
     h->p = compile_program(gates, n_gates, n_qubits, meas, n_meas, opts);
     build_tables(h);
+    const char* env = getenv("TEDQ_GB300_JIT");
+    const int mode = opts ? opts->jit : 0;
+    h->jit_on = mode > 0 || (mode == 0 && h->p->ns >= 14);
+    if (env && env[0] == '0') h->jit_on = false;
+    if (h->jit_on) {
+      h->jit_state = 1;
+      h->jit_srcs = jit_sources(*h->p);
+      const std::vector<JitSource>* srcs = &h->jit_srcs;
+      h->jit_future = std::async(std::launch::async, [srcs]() {
+        std::vector<std::string> cubins;
+        std::string err;
+        bool ok = jit_compile_all(*srcs, cubins, err);
+        return std::make_tuple(ok, std::move(cubins), std::move(err));
+      });
+    }
     *out = h;
     return TEDQ_OK;
   } catch (const UnsupportedError& e) {
@@ -163,6 +235,7 @@ int32_t tedq_program_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
 
 int32_t tedq_program_destroy(tedq_program_t* prog) {
   if (!prog) return TEDQ_OK;
+  if (prog->jit_future.valid()) prog->jit_future.wait();
   for (auto& ev : prog->events) {
     cudaEventDestroy(ev.a);
     cudaEventDestroy(ev.b);
@@ -189,6 +262,15 @@ int32_t tedq_program_info(const tedq_program_t* prog, tedq_program_info_t* info)
   info->n_elem_gates = (int32_t)p.elem.size();
   info->precision = p.precision;
   info->workspace_per_circuit = ws_layout(p, 1).total;
+  info->jit_state = prog->jit_state;
+  return TEDQ_OK;
+}
+
+int32_t tedq_program_jit_wait(tedq_program_t* prog) {
+  if (!prog) return fail(TEDQ_ERR_ARG, "tedq_program_jit_wait: program is null");
+  if (!prog->jit_on) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_program_jit_wait: specialised kernels are off");
+  std::lock_guard<std::mutex> lock(prog->jit_mu);
+  if (!jit_compiled(prog)) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_program_jit_wait: " + prog->jit_err);
   return TEDQ_OK;
 }
 
@@ -232,15 +314,21 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
     e = timed(prog, 0, 0, s, [&] { return launch_init_state(dbl, p.ns, p.pad, psi, init, batch, s); });
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/init");
   }
+  JitKernels* jk = p.fwd.passes.empty() ? nullptr : jit_kernels(prog);
   for (size_t i = 0; i < p.fwd.passes.size(); ++i) {
     if (i == 0) {
       PassParams P = p.fwd.passes[0];
       P.init = init ? 2 : 1;
       P.pad_bits = (uint8_t)p.pad;
-      e = timed(prog, 0, batch << p.ns, s, [&] { return launch_fwd_pass(dbl, P, psi, params, p.n_params, init, batch, s); });
+      e = timed(prog, 0, batch << p.ns, s, [&] {
+        return jk ? jit_launch_fwd(jk->fwd[0], dbl, P, psi, params, p.n_params, init, batch, s)
+                  : launch_fwd_pass(dbl, P, psi, params, p.n_params, init, batch, s);
+      });
     } else {
-      e = timed(prog, 0, batch << p.ns, s,
-                [&] { return launch_fwd_pass(dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s); });
+      e = timed(prog, 0, batch << p.ns, s, [&] {
+        return jk ? jit_launch_fwd(jk->fwd[i], dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s)
+                  : launch_fwd_pass(dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s);
+      });
     }
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/pass");
   }
@@ -302,9 +390,13 @@ int32_t tedq_run_adjoint(tedq_program_t* prog, const void* params, int64_t batch
                               batch, s);
   });
   if (e != cudaSuccess) return cuda_fail(e, "tedq_run_adjoint/lambda");
-  for (const PassParams& P : p.bwd.passes) {
-    e = timed(prog, 1, batch << p.ns, s,
-              [&] { return launch_bwd_pass(dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s); });
+  JitKernels* jk = jit_kernels(prog);
+  for (size_t i = 0; i < p.bwd.passes.size(); ++i) {
+    const PassParams& P = p.bwd.passes[i];
+    e = timed(prog, 1, batch << p.ns, s, [&] {
+      return jk ? jit_launch_bwd(jk->bwd[i], dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s)
+                : launch_bwd_pass(dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s);
+    });
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run_adjoint/pass");
   }
   e = timed(prog, 3, 0, s, [&] { return launch_grad_finalize(dbl, grad_acc, grad, batch * p.n_params, s); });

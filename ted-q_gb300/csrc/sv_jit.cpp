@@ -1,0 +1,412 @@
+// sv_jit.cpp -- generation, NVRTC compilation, caching and launch of the
+// per-circuit specialised pass kernels (see sv_jit.h).
+#include "sv_jit.h"
+
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+#include <algorithm>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <atomic>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <thread>
+
+#include "sv_program.h"
+
+namespace tedq {
+
+// ---------------------------------------------------------------- code generation
+
+static const char* real_of(const PassParams& P) { return P.e == 1 ? "float" : "double"; }
+
+static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r, const char* arr) {
+  const int R = P.R;
+  const char* real = real_of(P);
+  char buf[256];
+  auto cm = [](unsigned v) { return std::to_string(v) + "u"; };
+  switch (r.kind) {
+    case GK_U1:
+    case GK_D1:
+    case GK_RXT:
+    case GK_RYT:
+    case GK_PH: {
+      static const char* fn[] = {"apply_u1", "apply_d1", "", "", "apply_rxt", "apply_ryt", "apply_ph"};
+      snprintf(buf, sizeof buf, "  %s<%d, %d, %s>(%s, c.mats[%d], CM<%s>{});\n", fn[r.kind], r.k0, R, real, arr,
+               r.mat, cm(r.cmask).c_str());
+      o << buf;
+      break;
+    }
+    case GK_X:
+      snprintf(buf, sizeof buf, "  apply_x<%d, %d, %s>(%s, CM<%s>{});\n", r.k0, R, real, arr, cm(r.cmask).c_str());
+      o << buf;
+      break;
+    default: {  // GK_SWAP as three controlled bit flips
+      const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
+      const int tg[3] = {r.k1, r.k0, r.k1};
+      const unsigned c[3] = {r.cmask | b0, r.cmask | b1, r.cmask | b0};
+      for (int i = 0; i < 3; ++i) {
+        snprintf(buf, sizeof buf, "  apply_x<%d, %d, %s>(%s, CM<%s>{});\n", tg[i], R, real, arr, cm(c[i]).c_str());
+        o << buf;
+      }
+    }
+  }
+}
+
+static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
+  const char* real = real_of(P);
+  char buf[512];
+  if (!adjoint) {
+    snprintf(buf, sizeof buf,
+             "extern \"C\" __global__ void __launch_bounds__(256, 2) tedq_fwd_%d(\n"
+             "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
+             "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long circ0) {\n"
+             "  TEDQ_FWD_PROLOGUE(%s, %d)\n",
+             index, real, real, real, real, P.R);
+  } else {
+    snprintf(buf, sizeof buf,
+             "extern \"C\" __global__ void __launch_bounds__(256, 2) tedq_bwd_%d(\n"
+             "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
+             "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long circ0) {\n"
+             "  TEDQ_BWD_PROLOGUE(%s, %d)\n",
+             index, real, real, real, real, P.R);
+  }
+  o << buf;
+  for (int f = 0; f < P.n_phases; ++f) {
+    const Phase& ph = P.phase[f];
+    if (ph.type != PH_REG) {
+      o << "  c.dense(" << f << ");\n";
+      continue;
+    }
+    o << "  c.begin(" << f << ");\n";
+    for (int g = ph.g0; g < ph.g1; ++g) {
+      const RGate& r = P.gate[g];
+      if (adjoint && r.grad != GR_NONE) {
+        static const char* gn[] = {"", "GR_X", "GR_Y", "GR_Z", "GR_P1"};
+        snprintf(buf, sizeof buf, "  c.grad(%d, grad_part<%s, %d, %d, %s>(c.a, c.l, CM<%uu>{}), %.9ef);\n", g,
+                 gn[r.grad], r.k0, P.R, real, (unsigned)r.cmask, (double)r.coef);
+        o << buf;
+      }
+      emit_gate(o, P, r, "c.a");
+      if (adjoint) emit_gate(o, P, r, "c.l");
+    }
+    o << "  c.end(" << f << ");\n";
+  }
+  o << "  c.finish();\n}\n\n";
+}
+
+std::vector<JitSource> jit_sources(const Program& p) {
+  std::vector<JitSource> out;
+  auto one = [&](const PassParams& P, int i, bool adjoint) {
+    std::ostringstream o;
+    o << "// generated by tedq_gb300: specialised pass kernel of one compiled circuit\n"
+         "#include \"sv_device.cuh\"\n"
+         "using namespace tedq;\nusing namespace tedq::dev;\n\n";
+    emit_pass(o, P, i, adjoint);
+    out.push_back({(adjoint ? "tedq_bwd_" : "tedq_fwd_") + std::to_string(i), o.str()});
+  };
+  for (size_t i = 0; i < p.fwd.passes.size(); ++i) one(p.fwd.passes[i], (int)i, false);
+  for (size_t i = 0; i < p.bwd.passes.size(); ++i) one(p.bwd.passes[i], (int)i, true);
+  return out;
+}
+
+// ---------------------------------------------------------------- NVRTC
+
+#include "jit_headers.inc"  // kJitHeaderNames / kJitHeaderSrc (generated by build.py)
+
+namespace {
+
+struct Nvrtc {
+  bool ok = false;
+  std::string why;
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) cubin = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcVersion) version = nullptr;
+  decltype(&nvrtcGetErrorString) errstr = nullptr;
+};
+
+Nvrtc load_nvrtc() {
+  Nvrtc n;
+  std::vector<std::string> cands = {"libnvrtc.so.13", "libnvrtc.so"};
+  for (const char* env : {"CUDA_HOME", "CUDA_PATH"})
+    if (const char* d = getenv(env)) cands.push_back(std::string(d) + "/lib64/libnvrtc.so.13");
+  cands.push_back("/usr/local/cuda/lib64/libnvrtc.so.13");
+  void* h = nullptr;
+  for (auto& c : cands)
+    if ((h = dlopen(c.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) {
+    n.why = "libnvrtc.so.13 not found";
+    return n;
+  }
+#define TEDQ_SYM(field, name)                                  \
+  n.field = reinterpret_cast<decltype(n.field)>(dlsym(h, name)); \
+  if (!n.field) {                                              \
+    n.why = std::string("missing symbol ") + name;             \
+    return n;                                                  \
+  }
+  TEDQ_SYM(create, "nvrtcCreateProgram")
+  TEDQ_SYM(compile, "nvrtcCompileProgram")
+  TEDQ_SYM(log_size, "nvrtcGetProgramLogSize")
+  TEDQ_SYM(log, "nvrtcGetProgramLog")
+  TEDQ_SYM(cubin_size, "nvrtcGetCUBINSize")
+  TEDQ_SYM(cubin, "nvrtcGetCUBIN")
+  TEDQ_SYM(destroy, "nvrtcDestroyProgram")
+  TEDQ_SYM(version, "nvrtcVersion")
+  TEDQ_SYM(errstr, "nvrtcGetErrorString")
+#undef TEDQ_SYM
+  n.ok = true;
+  return n;
+}
+
+Nvrtc& nvrtc() {
+  static Nvrtc n = load_nvrtc();
+  return n;
+}
+
+uint64_t fnv1a(uint64_t h, const std::string& s) {
+  for (unsigned char ch : s) {
+    h ^= ch;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+std::string cache_dir() {
+  if (const char* d = getenv("TEDQ_GB300_CACHE")) return d;
+  if (const char* home = getenv("HOME")) return std::string(home) + "/.cache/tedq_gb300";
+  return "/tmp/tedq_gb300_cache";
+}
+
+void mkdirs(const std::string& path) {
+  std::string cur;
+  for (size_t i = 0; i < path.size(); ++i) {
+    cur += path[i];
+    if (path[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+  }
+  mkdir(path.c_str(), 0755);
+}
+
+const char* const kOptions[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo", "-DNDEBUG"};
+
+}  // namespace
+
+bool jit_compile(const std::string& src, std::string& cubin, std::string& err) {
+  Nvrtc& N = nvrtc();
+  if (!N.ok) {
+    err = "NVRTC unavailable: " + N.why;
+    return false;
+  }
+  int major = 0, minor = 0;
+  N.version(&major, &minor);
+  uint64_t key = 1469598103934665603ull;
+  key = fnv1a(key, src);
+  for (int i = 0; i < 2; ++i) key = fnv1a(key, kJitHeaderSrc[i]);
+  for (const char* opt : kOptions) key = fnv1a(key, opt);
+  key = fnv1a(key, std::to_string(major) + "." + std::to_string(minor));
+  char name[64];
+  snprintf(name, sizeof name, "/pass_%016llx.cubin", (unsigned long long)key);
+  const std::string dir = cache_dir(), path = dir + name;
+  {
+    std::ifstream in(path, std::ios::binary);
+    if (in) {
+      std::stringstream ss;
+      ss << in.rdbuf();
+      cubin = ss.str();
+      if (!cubin.empty()) return true;
+    }
+  }
+  nvrtcProgram prog;
+  nvrtcResult r = N.create(&prog, src.c_str(), "tedq_passes.cu", 2, kJitHeaderSrc, kJitHeaderNames);
+  if (r != NVRTC_SUCCESS) {
+    err = std::string("nvrtcCreateProgram: ") + N.errstr(r);
+    return false;
+  }
+  std::vector<const char*> opts(kOptions, kOptions + sizeof(kOptions) / sizeof(kOptions[0]));
+  const bool verbose = getenv("TEDQ_GB300_JIT_VERBOSE") != nullptr;
+  if (verbose) opts.push_back("--ptxas-options=-v");
+  r = N.compile(prog, (int)opts.size(), opts.data());
+  if (verbose && r == NVRTC_SUCCESS) {
+    size_t n = 0;
+    N.log_size(prog, &n);
+    std::string log(n, '\0');
+    if (n) N.log(prog, &log[0]);
+    fprintf(stderr, "%s\n", log.c_str());
+  }
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    N.log_size(prog, &n);
+    std::string log(n, '\0');
+    if (n) N.log(prog, &log[0]);
+    err = std::string("nvrtcCompileProgram: ") + N.errstr(r) + "\n" + log.substr(0, 4000);
+    N.destroy(&prog);
+    return false;
+  }
+  size_t sz = 0;
+  N.cubin_size(prog, &sz);
+  cubin.assign(sz, '\0');
+  N.cubin(prog, &cubin[0]);
+  N.destroy(&prog);
+  mkdirs(dir);
+  const std::string tmp = path + ".tmp." + std::to_string(getpid());
+  {
+    std::ofstream out(tmp, std::ios::binary);
+    out.write(cubin.data(), (std::streamsize)cubin.size());
+  }
+  rename(tmp.c_str(), path.c_str());
+  return true;
+}
+
+bool jit_compile_all(const std::vector<JitSource>& srcs, std::vector<std::string>& cubins, std::string& err) {
+  cubins.assign(srcs.size(), std::string());
+  std::vector<std::string> errs(srcs.size());
+  std::atomic<size_t> next(0);
+  std::atomic<bool> ok(true);
+  unsigned hw = std::thread::hardware_concurrency();
+  if (const char* e = getenv("TEDQ_GB300_JIT_THREADS")) hw = (unsigned)atoi(e);
+  const size_t nthreads = std::max<size_t>(1, std::min<size_t>(srcs.size(), hw ? hw : 4));
+  auto work = [&]() {
+    for (size_t i = next++; i < srcs.size() && ok; i = next++)
+      if (!jit_compile(srcs[i].src, cubins[i], errs[i])) ok = false;
+  };
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < nthreads; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  if (!ok)
+    for (size_t i = 0; i < srcs.size(); ++i)
+      if (!errs[i].empty()) {
+        err = srcs[i].name + ": " + errs[i];
+        break;
+      }
+  return ok;
+}
+
+// ---------------------------------------------------------------- loading and launch
+// Driver functions are reached through cudaGetDriverEntryPointByVersion, so
+// the library needs no link-time dependency on libcuda.
+
+namespace {
+
+struct Driver {
+  bool ok = false;
+  std::string why;
+  decltype(&cuModuleLoadData) load = nullptr;
+  decltype(&cuModuleGetFunction) get = nullptr;
+  decltype(&cuFuncSetAttribute) set_attr = nullptr;
+  decltype(&cuLaunchKernel) launch = nullptr;
+};
+
+template <typename F>
+bool entry(const char* name, F& fn, std::string& why) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p) {
+    why = std::string("driver entry point ") + name + " unavailable";
+    return false;
+  }
+  fn = reinterpret_cast<F>(p);
+  return true;
+}
+
+Driver load_driver() {
+  Driver d;
+  if (!entry("cuModuleLoadData", d.load, d.why) || !entry("cuModuleGetFunction", d.get, d.why) ||
+      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why))
+    return d;
+  d.ok = true;
+  return d;
+}
+
+Driver& driver() {
+  static std::once_flag once;
+  static Driver d;
+  std::call_once(once, [] { d = load_driver(); });
+  return d;
+}
+
+constexpr int kMaxGridY = 65535;
+
+}  // namespace
+
+bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSource>& srcs, int n_fwd, int n_bwd,
+              JitKernels& out, std::string& err) {
+  Driver& D = driver();
+  if (!D.ok) {
+    err = D.why;
+    return false;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaSetDevice(dev) != cudaSuccess) {
+    err = "no current CUDA device";
+    return false;
+  }
+  if ((int)cubins.size() != n_fwd + n_bwd || srcs.size() != cubins.size()) {
+    err = "kernel count mismatch";
+    return false;
+  }
+  for (size_t i = 0; i < cubins.size(); ++i) {
+    CUmodule mod = nullptr;
+    CUresult r = D.load(&mod, cubins[i].data());
+    if (r != CUDA_SUCCESS) {
+      err = "cuModuleLoadData failed (" + std::to_string((int)r) + ")";
+      return false;
+    }
+    out.modules.push_back(mod);
+    CUfunction f = nullptr;
+    if (D.get(&f, mod, srcs[i].name.c_str()) != CUDA_SUCCESS) {
+      err = "missing kernel " + srcs[i].name;
+      return false;
+    }
+    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 64 * 1024);
+    ((int)i < n_fwd ? out.fwd : out.bwd).push_back(reinterpret_cast<void*>(f));
+  }
+  return true;
+}
+
+static cudaError_t to_rt(CUresult r) { return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure; }
+
+cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
+                           const void* init, int64_t batch, cudaStream_t s) {
+  const int E = dbl ? 0 : 1;
+  const unsigned smem = 16u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
+  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
+    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
+    long long circ0 = c0;
+    void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
+                    const_cast<void**>(&init), &circ0};
+    CUresult r = driver().launch(reinterpret_cast<CUfunction>(fn), tiles, (unsigned)nb, 1, T, 1, 1, smem,
+                                 reinterpret_cast<CUstream>(s), args, nullptr);
+    if (r != CUDA_SUCCESS) return to_rt(r);
+  }
+  return cudaSuccess;
+}
+
+cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
+                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
+  const int E = dbl ? 0 : 1;
+  const unsigned smem = 32u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
+  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
+    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
+    long long circ0 = c0;
+    void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
+                    &circ0};
+    CUresult r = driver().launch(reinterpret_cast<CUfunction>(fn), tiles, (unsigned)nb, 1, T, 1, 1, smem,
+                                 reinterpret_cast<CUstream>(s), args, nullptr);
+    if (r != CUDA_SUCCESS) return to_rt(r);
+  }
+  return cudaSuccess;
+}
+
+}  // namespace tedq

@@ -44,7 +44,8 @@ class Meas(ctypes.Structure):
 
 
 class Options(ctypes.Structure):
-    _fields_ = [("precision", c_int32), ("fuse", c_int32), ("tile_qubits", c_int32), ("reserved", c_int32 * 5)]
+    _fields_ = [("precision", c_int32), ("fuse", c_int32), ("tile_qubits", c_int32), ("jit", c_int32),
+                ("reserved", c_int32 * 4)]
 
 
 class ProgramInfo(ctypes.Structure):
@@ -52,7 +53,8 @@ class ProgramInfo(ctypes.Structure):
                 ("n_real_outputs", c_int32), ("n_terms", c_int32), ("n_fwd_passes", c_int32),
                 ("n_bwd_passes", c_int32), ("n_fwd_phases", c_int32), ("n_bwd_phases", c_int32),
                 ("n_fused_gates", c_int32), ("n_elem_gates", c_int32), ("precision", c_int32),
-                ("workspace_per_circuit", c_int64), ("reserved", c_int64 * 4)]
+                ("workspace_per_circuit", c_int64), ("jit_state", c_int32), ("pad", c_int32),
+                ("reserved", c_int64 * 3)]
 
 
 class Profile(ctypes.Structure):
@@ -70,6 +72,7 @@ SIGNATURES = {
     "tedq_program_destroy": (c_int32, [c_void_p]),
     "tedq_program_info": (c_int32, [c_void_p, POINTER(ProgramInfo)]),
     "tedq_program_workspace_bytes": (c_int64, [c_void_p, c_int64]),
+    "tedq_program_jit_wait": (c_int32, [c_void_p]),
     "tedq_program_describe": (c_int64, [c_void_p, c_int32, c_char_p, c_int64]),
     "tedq_run": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                            c_void_p]),

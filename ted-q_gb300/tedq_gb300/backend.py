@@ -54,7 +54,7 @@ def _cmatrix(m, k):
 class NativeProgram:
     """Owner of one ``tedq_program_t`` (compile of a recorded circuit)."""
 
-    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0):
+    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0, jit=0):
         L = _lib.lib()
         self.n = int(circuit.num_qubits)
         ops = list(circuit.operators)
@@ -150,6 +150,7 @@ class NativeProgram:
         opts.precision = _lib.PREC_C128 if precision == "c128" else _lib.PREC_C64
         opts.fuse = 1 if fuse else 0
         opts.tile_qubits = int(tile_qubits)
+        opts.jit = int(jit)
         h = ctypes.c_void_p()
         _lib.check(L.tedq_program_create(gates, len(ops), self.n, M, len(meas), ctypes.byref(opts), ctypes.byref(h)),
                    "tedq_program_create")
@@ -180,6 +181,13 @@ class NativeProgram:
         buf = ctypes.create_string_buffer(int(need))
         L.tedq_program_describe(self.handle, int(adjoint), buf, need)
         return json.loads(buf.value.decode())
+
+    def jit_wait(self):
+        """Blocks until the specialised kernels are compiled; returns None when
+        they are ready, else the reason they are not used."""
+        L = _lib.lib()
+        st = L.tedq_program_jit_wait(self.handle)
+        return None if st == _lib.OK else _lib.last_error()
 
     def workspace_bytes(self, batch):
         return int(_lib.lib().tedq_program_workspace_bytes(self.handle, int(batch)))
@@ -314,7 +322,7 @@ class GB300Backend:
         self._measurements = circuit.measurements
         self._init_state = circuit.init_state
         self._prog = NativeProgram(circuit, self._precision, fuse=kwargs.get("fuse", True),
-                                   tile_qubits=kwargs.get("tile_qubits", 0))
+                                   tile_qubits=kwargs.get("tile_qubits", 0), jit=kwargs.get("jit", 0))
         self._ws = _Workspace()
         self._device = None
         self._init_dev = None

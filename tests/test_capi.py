@@ -91,3 +91,15 @@ def test_backend_compile_errors_match_reference():
     with pytest.raises(ValueError, match="number of parameters"):
         import torch
         cc(torch.tensor([0.1, 0.2, 0.3]))
+
+
+def test_specialised_kernels_compile_for_sm103a(tmp_path, monkeypatch):
+    """The per-circuit kernels generated for a circuit with every gate kind
+    compile with NVRTC for sm_103a (host only)."""
+    monkeypatch.setenv("TEDQ_GB300_CACHE", str(tmp_path))
+    from conftest import load_cases
+    case = next(c for c in load_cases() if c["name"] == "all_gates_n5")
+    for precision in ("c64", "c128"):
+        cc = qai.Circuit.from_spec(case).compilecircuit(backend="gb300", precision=precision, jit=1)
+        assert cc._prog.jit_wait() is None
+    assert any(p.suffix == ".cubin" for p in tmp_path.iterdir())

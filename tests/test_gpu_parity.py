@@ -41,10 +41,13 @@ def _native_loaded():
     assert qai._lib._lib is not None, "native library was not used"
 
 
+@pytest.mark.parametrize("jit", [-1, 1], ids=["generic", "specialised"])
 @pytest.mark.parametrize("precision", ["c64", "c128"])
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
-def test_forward_matches_reference(case, precision):
-    cc = _compile(case, precision)
+def test_forward_matches_reference(case, precision, jit):
+    cc = _compile(case, precision, jit=jit)
+    if jit == 1:
+        assert cc._prog.jit_wait() is None
     p = torch.tensor(case["params"], dtype=_rdt(precision), device=DEV)
     out = cc(p) if case["params"] else cc()
     assert list(out.shape) == case["shape"]
@@ -59,10 +62,11 @@ def test_forward_matches_reference(case, precision):
 GRAD_CASES = [c for c in CASES if c["params"]]
 
 
+@pytest.mark.parametrize("jit", [-1, 1], ids=["generic", "specialised"])
 @pytest.mark.parametrize("precision", ["c64", "c128"])
 @pytest.mark.parametrize("case", GRAD_CASES, ids=[c["name"] for c in GRAD_CASES])
-def test_adjoint_grad_matches_backprop(case, precision):
-    cc = _compile(case, precision)
+def test_adjoint_grad_matches_backprop(case, precision, jit):
+    cc = _compile(case, precision, jit=jit)
     p = torch.tensor(case["params"], dtype=_rdt(precision), device=DEV, requires_grad=True)
     out = cc(p)
     dy = torch.tensor(case["dy"], dtype=torch.float64, device=DEV).reshape(out.shape)
@@ -121,11 +125,12 @@ def _vqc_spec(n, layers, seed):
     return {"n": n, "gates": gates, "meas": meas, "init_state": None}
 
 
+@pytest.mark.parametrize("jit", [-1, 1], ids=["generic", "specialised"])
 @pytest.mark.parametrize("n,layers", [(14, 3), (20, 10)])
-def test_batched_vqc_against_oracle(n, layers):
+def test_batched_vqc_against_oracle(n, layers, jit):
     """Multi-pass circuits in a batch, value and adjoint gradient vs the complex128 oracle."""
     spec = _vqc_spec(n, layers, seed=n)
-    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300")
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=jit)
     P = cc.num_params
     gen = torch.Generator().manual_seed(n)
     params = torch.rand(3, P, generator=gen, dtype=torch.float64) * 2 * np.pi
