@@ -274,7 +274,8 @@ def run_ours(a):
 
     spec = vqc_spec(a.qubits, a.layers)
     t_compile = time.perf_counter()
-    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain, jit=a.jit)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain, jit=a.jit,
+                                                    tile_qubits=a.tile)
     jit_reason = cc._prog.jit_wait()
     t_compile = time.perf_counter() - t_compile
     info = cc.program_info
@@ -409,6 +410,7 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
+    ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)

@@ -554,7 +554,6 @@ struct BwdPass {
     sl = lam + (circ << P.n);
     const real* prm = params ? params + circ * n_params : nullptr;
     for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
-    for (int i = tid; i < P.n_gates; i += T) gacc[i] = 0.0;
     gthr = tile_base(P, blockIdx.x);
     sthr = 0;
     thread_offsets(P, tid, P.m - R, gthr, sthr);
@@ -606,11 +605,50 @@ struct BwdPass {
     __syncthreads();
   }
 
-  // Warp-reduce one gate's partial gradient and add it to the CTA accumulator.
-  __device__ __forceinline__ void grad(int g, real part, float coef) {
+  // Warp-reduce one gate's partial gradient into this warp's slot of gate g
+  // (each slot is written by one lane of one warp: no atomics).
+  __device__ __forceinline__ void grad(int g, real part) {
 #pragma unroll
     for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-    if ((tid & 31) == 0) atomicAdd(&gacc[g], (double)part * (double)coef);
+    if ((tid & 31) == 0) gacc[(tid >> 5) * kMaxPassGates + g] = (double)part;
+  }
+
+  // Eight gates at once: a transposed butterfly leaves the warp sum of value
+  // j on lanes 4j..4j+3 after 9 shuffles (instead of 8 x 5); gate index < 0
+  // marks an unused value.
+  __device__ __forceinline__ void grad8(real v0, real v1, real v2, real v3, real v4, real v5, real v6, real v7,
+                                        int g0, int g1, int g2, int g3, int g4, int g5, int g6, int g7) {
+    const unsigned lane = tid & 31;
+    real v[8] = {v0, v1, v2, v3, v4, v5, v6, v7};
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const real send = b4 ? v[j] : v[j + 4];
+      const real keep = b4 ? v[j + 4] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const real send = b3 ? v[j] : v[j + 2];
+      const real keep = b3 ? v[j + 2] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    {
+      const real send = b2 ? v[0] : v[1];
+      const real keep = b2 ? v[1] : v[0];
+      v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    if ((lane & 3) == 0) {
+      const int which = (b4 ? 4 : 0) + (b3 ? 2 : 0) + (b2 ? 1 : 0);
+      const int gs[8] = {g0, g1, g2, g3, g4, g5, g6, g7};
+      int g = gs[0];
+#pragma unroll
+      for (int j = 1; j < 8; ++j)
+        if (which == j) g = gs[j];
+      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = (double)v[0];
+    }
   }
 
   __device__ __forceinline__ void dense(int f) {
@@ -627,9 +665,14 @@ struct BwdPass {
       reinterpret_cast<U*>(sl)[g] = tl[sthr ^ P.sk[k]];
     }
     if (P.n_grad) {
+      __syncthreads();
+      const int nw = blockDim.x >> 5;
       for (int g = tid; g < P.n_gates; g += blockDim.x) {
         const int32_t slot = P.gate[g].slot;
-        if (slot >= 0) atomicAdd(&grad_acc[circ * n_params + slot], gacc[g]);
+        if (slot < 0) continue;
+        double sum = 0.0;
+        for (int w = 0; w < nw; ++w) sum += gacc[w * kMaxPassGates + g];
+        atomicAdd(&grad_acc[circ * n_params + slot], sum * (double)P.gate[g].coef);
       }
     }
   }
@@ -648,6 +691,6 @@ struct BwdPass {
 #define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                  \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  __shared__ double tedq_gacc[tedq::kMaxPassGates];                                                  \
+  __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                                  \
   tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::Unit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);

@@ -78,6 +78,17 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
              index, real, real, real, real, P.R);
   }
   o << buf;
+  int var = 0;
+  std::vector<std::pair<std::string, int>> pending;  // gradient partials not yet reduced
+  auto flush = [&]() {
+    if (pending.empty()) return;
+    o << "  c.grad8(";
+    for (int j = 0; j < 8; ++j)
+      o << (j ? ", " : "") << (j < (int)pending.size() ? pending[j].first : std::string("(") + real + ")0");
+    for (int j = 0; j < 8; ++j) o << ", " << (j < (int)pending.size() ? pending[j].second : -1);
+    o << ");\n";
+    pending.clear();
+  };
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
     if (ph.type != PH_REG) {
@@ -89,13 +100,17 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
       const RGate& r = P.gate[g];
       if (adjoint && r.grad != GR_NONE) {
         static const char* gn[] = {"", "GR_X", "GR_Y", "GR_Z", "GR_P1"};
-        snprintf(buf, sizeof buf, "  c.grad(%d, grad_part<%s, %d, %d, %s>(c.a, c.l, CM<%uu>{}), %.9ef);\n", g,
-                 gn[r.grad], r.k0, P.R, real, (unsigned)r.cmask, (double)r.coef);
+        const std::string v = "gv" + std::to_string(var++);
+        snprintf(buf, sizeof buf, "  const %s %s = grad_part<%s, %d, %d, %s>(c.a, c.l, CM<%uu>{});\n", real,
+                 v.c_str(), gn[r.grad], r.k0, P.R, real, (unsigned)r.cmask);
         o << buf;
+        pending.push_back({v, g});
+        if (pending.size() == 8) flush();
       }
       emit_gate(o, P, r, "c.a");
       if (adjoint) emit_gate(o, P, r, "c.l");
     }
+    flush();
     o << "  c.end(" << f << ");\n";
   }
   o << "  c.finish();\n}\n\n";

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256, 2)
       c.begin(f);
       for (int g = ph.g0; g < ph.g1; ++g) {
         const RGate& r = P.gate[g];
-        if (r.grad != GR_NONE) c.grad(g, dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask), r.coef);
+        if (r.grad != GR_NONE) c.grad(g, dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask));
         dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
         dev::apply_rgate<R, real>(r, c.l, c.mats[r.mat]);
       }
@@ -121,33 +121,86 @@ __device__ __forceinline__ real term_value(const TermDev& t, cpx<real> v, cpx<re
   }
 }
 
+// 16-point Walsh-Hadamard transform in registers: h[k] <- sum_j h[j] (-1)^{popc(k & j)}.
+template <typename real>
+__device__ __forceinline__ void wht16(real* h) {
+#pragma unroll
+  for (int len = 1; len < 16; len <<= 1)
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (!(i & len)) {
+        const real a = h[i], b = h[i | len];
+        h[i] = a + b;
+        h[i | len] = a - b;
+      }
+}
+
+// 16 consecutive amplitudes starting at a multiple of 16 (vector loads).
+template <typename real>
+__device__ __forceinline__ void load16(const cpx<real>* st, uint64_t w0, cpx<real>* v) {
+  constexpr int E = kE<real>;
+  const Unit<real>* u = reinterpret_cast<const Unit<real>*>(st + w0);
+  Unit<real> x[16 >> E];
+#pragma unroll
+  for (int k = 0; k < (16 >> E); ++k) x[k] = u[k];
+#pragma unroll
+  for (int k = 0; k < (16 >> E); ++k)
+#pragma unroll
+    for (int e = 0; e < (1 << E); ++e) v[(k << E) + e] = x[k].v[e];
+}
+
+// Pauli-string expectations.  Each thread takes 16 consecutive amplitudes
+// w0..w0+15; for a diagonal string Z^z the chunk contributes
+// (-1)^{popc(z & w0)} * WHT(|psi|^2)[z & 15], one shared-memory lookup per
+// string after one 16-point transform.  Off-diagonal strings (X/Y factors)
+// read the partner amplitudes directly.  FP32 per thread and warp, FP64 across.
 template <typename real>
 __global__ void __launch_bounds__(kMeasThreads)
     expval_kernel(const __grid_constant__ TermTable TT, const cpx<real>* __restrict__ psi, int n,
                   double* __restrict__ acc, int64_t circ0) {
+  __shared__ real hs[16][kMeasThreads];
   __shared__ double sacc[32];
   const int tid = threadIdx.x, lane = tid & 31;
   const int64_t circ = circ0 + blockIdx.y;
   const uint64_t N = 1ull << n;
   const cpx<real>* st = psi + circ * (int64_t)N;
-  const uint64_t w0 = (uint64_t)blockIdx.x * kMeasChunk;
-  const uint64_t w1 = w0 + kMeasChunk < N ? w0 + kMeasChunk : N;
+  const uint64_t w0 = (uint64_t)blockIdx.x * kMeasChunk + (uint64_t)tid * 16;
+  const bool valid = w0 < N;
+  cpx<real> v[16];
+  if (valid) {
+    load16<real>(st, w0, v);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = mk<real>((real)0, (real)0);
+  }
+  {
+    real h[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) h[j] = v[j].x * v[j].x + v[j].y * v[j].y;
+    wht16<real>(h);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) hs[j][tid] = h[j];
+  }
   for (int sg = 0; sg < TT.n; sg += 32) {
     if (tid < 32) sacc[tid] = 0.0;
     __syncthreads();
     real part[32];
 #pragma unroll
-    for (int s = 0; s < 32; ++s) part[s] = 0;
-    for (uint64_t w = w0 + tid; w < w1; w += kMeasThreads) {
-      const cpx<real> v = st[w];
-      const real p = v.x * v.x + v.y * v.y;
-#pragma unroll
-      for (int s = 0; s < 32; ++s) {
-        if (sg + s < TT.n) {
-          const TermDev& t = TT.t[sg + s];
-          const real sgn = (__popcll(t.z & w) & 1) ? (real)-1 : (real)1;
-          if (t.x == 0) part[s] += sgn * p;
-          else part[s] += sgn * term_value<real>(t, v, st[w ^ t.x]);
+    for (int s = 0; s < 32; ++s) {
+      part[s] = 0;
+      if (sg + s < TT.n) {
+        const TermDev& t = TT.t[sg + s];
+        if (t.x == 0) {
+          const real hv = hs[t.z & 15][tid];
+          part[s] = (__popcll(t.z & w0) & 1) ? -hv : hv;
+        } else if (valid) {
+          real q = 0;
+          for (int j = 0; j < 16; ++j) {
+            const uint64_t w = w0 + j;
+            const real tv = term_value<real>(t, v[j], st[w ^ t.x]);
+            q += (__popcll(t.z & w) & 1) ? -tv : tv;
+          }
+          part[s] = q;
         }
       }
     }
@@ -254,28 +307,66 @@ __global__ void term_weights_kernel(const __grid_constant__ OutTermTable O, cons
   w[i] = v;
 }
 
+// lambda = sum_s w_s P_s psi + (probs weights) psi + dy_state / 2, in chunks of
+// 16 consecutive amplitudes: the diagonal strings' weights are scattered to
+// D[z & 15] with the sign of the chunk's high bits, and one inverse 16-point
+// Walsh-Hadamard transform gives the diagonal multiplier of every amplitude.
 template <typename real>
 __global__ void __launch_bounds__(256)
     lambda_init_kernel(const __grid_constant__ TermTable TT, const __grid_constant__ ProbsTable PT,
                        const double* __restrict__ wts, const real* __restrict__ dy, int n_real,
                        const cpx<real>* __restrict__ dys, const cpx<real>* __restrict__ psi, cpx<real>* __restrict__ lam,
                        int n, int64_t circ0) {
+  constexpr int E = kE<real>;
+  __shared__ real ds[16][256];
+  __shared__ real wsm[kMaxTerms];
+  const int tid = threadIdx.x;
   const int64_t circ = circ0 + blockIdx.y;
   const uint64_t N = 1ull << n;
   const cpx<real>* st = psi + circ * (int64_t)N;
+  cpx<real>* lt = lam + circ * (int64_t)N;
   const uint64_t padm = (1ull << PT.pad_bits) - 1;
-  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < N; w += (uint64_t)gridDim.x * blockDim.x) {
-    const cpx<real> v = st[w];
-    real d = 0;
-    cpx<real> acc = mk<real>((real)0, (real)0);
+  for (int s = tid; s < TT.n; s += blockDim.x) wsm[s] = (real)wts[circ * TT.n + s];
+  __syncthreads();
+  for (uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + tid) * 16; w0 < N;
+       w0 += (uint64_t)gridDim.x * blockDim.x * 16) {
+    cpx<real> v[16];
+    load16<real>(st, w0, v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) ds[j][tid] = 0;
     for (int s = 0; s < TT.n; ++s) {
-      const real W = (real)wts[circ * TT.n + s];
-      if (W == (real)0) continue;
       const TermDev& t = TT.t[s];
-      const real sgn = (__popcll(t.z & w) & 1) ? -W : W;
-      if (t.x == 0) {
-        d += sgn;
-      } else {
+      const real W = wsm[s];
+      if (t.x == 0 && W != (real)0) ds[t.z & 15][tid] += (__popcll(t.z & w0) & 1) ? -W : W;
+    }
+    real d[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) d[j] = ds[j][tid];
+    wht16<real>(d);
+    if (dy) {
+      for (int pi = 0; pi < PT.n; ++pi) {
+        const ProbsDesc& pd = PT.p[pi];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const uint64_t w = w0 + j;
+          if (pd.full) {
+            if ((w & padm) == 0) d[j] += dy[circ * n_real + pd.offset + (w >> PT.pad_bits)];
+          } else {
+            d[j] += dy[circ * n_real + pd.offset + bin_of(pd, w)];
+          }
+        }
+      }
+    }
+    cpx<real> r[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) r[j] = mk<real>(d[j] * v[j].x, d[j] * v[j].y);
+    for (int s = 0; s < TT.n; ++s) {
+      const TermDev& t = TT.t[s];
+      const real W = wsm[s];
+      if (t.x == 0 || W == (real)0) continue;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const uint64_t w = w0 + j;
         const cpx<real> u = st[w ^ t.x];
         cpx<real> pu;
         switch (t.ny & 3) {
@@ -284,27 +375,27 @@ __global__ void __launch_bounds__(256)
           case 2: pu = mk<real>(-u.x, -u.y); break;
           default: pu = mk<real>(-u.y, u.x); break;
         }
-        acc.x += sgn * pu.x;
-        acc.y += sgn * pu.y;
+        const real sgn = (__popcll(t.z & w) & 1) ? -W : W;
+        r[j].x += sgn * pu.x;
+        r[j].y += sgn * pu.y;
       }
     }
-    if (dy) {
-      for (int pi = 0; pi < PT.n; ++pi) {
-        const ProbsDesc& pd = PT.p[pi];
-        if (pd.full) {
-          if ((w & padm) == 0) d += dy[circ * n_real + pd.offset + (w >> PT.pad_bits)];
-        } else {
-          d += dy[circ * n_real + pd.offset + bin_of(pd, w)];
-        }
-      }
-    }
-    cpx<real> r = mk<real>(d * v.x + acc.x, d * v.y + acc.y);
     if (dys) {
-      const cpx<real> g = dys[circ * (int64_t)N + w];
-      r.x += (real)0.5 * g.x;
-      r.y += (real)0.5 * g.y;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const cpx<real> g = dys[circ * (int64_t)N + w0 + j];
+        r[j].x += (real)0.5 * g.x;
+        r[j].y += (real)0.5 * g.y;
+      }
     }
-    lam[circ * (int64_t)N + w] = r;
+    Unit<real>* out = reinterpret_cast<Unit<real>*>(lt + w0);
+#pragma unroll
+    for (int k = 0; k < (16 >> E); ++k) {
+      Unit<real> x;
+#pragma unroll
+      for (int e = 0; e < (1 << E); ++e) x.v[e] = r[(k << E) + e];
+      out[k] = x;
+    }
   }
 }
 
@@ -426,7 +517,8 @@ template <typename real>
 cudaError_t lambda_impl(int n, const TermTable& TT, const ProbsTable& PT, const double* w, const void* dy,
                         int n_real, const void* dys, const void* psi, void* lam, int64_t batch, cudaStream_t s) {
   const uint64_t N = 1ull << n;
-  const unsigned bx = (unsigned)((N + 255) / 256 < 8192 ? (N + 255) / 256 : 8192);
+  const uint64_t chunks = (N + 16 * 256 - 1) / (16 * 256);
+  const unsigned bx = (unsigned)(chunks < 8192 ? chunks : 8192);
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     lambda_init_kernel<real><<<dim3(bx, (unsigned)nb), 256, 0, s>>>(
