@@ -399,6 +399,74 @@ def run_ours(a):
     return 0
 
 
+# ---------------------------------------------------------------- serving stream
+
+def run_serving(a):
+    """Serving stream: Poisson arrivals of value+grad evaluations of the
+    hardware-efficient ansatz, n uniform over {4,8,12,16,20,24}, depth uniform
+    in [2, 12], swept over arrival rates; throughput and p50/p99 latency per
+    qubit bucket.  Specialised kernels compile in the background while the
+    generic kernels serve."""
+    import threading
+    import tedq_gb300 as qai
+    from tedq_gb300.serving import Server
+    from tedq_gb300.templates import hea_spec
+    torch.cuda.set_device(0)
+    sizes, depths = [4, 8, 12, 16, 20, 24], list(range(2, 13))
+    progs = {(n, d): qai.Circuit.from_spec(hea_spec(n, d)).compilecircuit(backend="gb300", jit=2)
+             for n in sizes for d in depths}
+    rng = np.random.default_rng(2024)
+    rates = [float(r) for r in a.rates.split(",")]
+    results = []
+    with Server(max_batch=64, max_wait_us=300, memory_budget_bytes=int(a.budget_gb * (1 << 30)),
+                n_streams=8) as srv:
+        # warm-up: every program once (loads modules, touches the arena)
+        for cc in progs.values():
+            srv.wait(srv.submit(cc, np.zeros(cc.num_params, np.float32)), timeout_s=600)
+        for lam in rates:
+            n_req = max(20, int(lam * a.duration))
+            gaps = rng.exponential(1.0 / lam, n_req)
+            keys = [(sizes[rng.integers(6)], depths[rng.integers(11)]) for _ in range(n_req)]
+            params = [rng.uniform(0, 2 * np.pi, progs[k].num_params).astype(np.float32) for k in keys]
+            tickets = [None] * n_req
+            t0 = time.perf_counter()
+
+            def producer():
+                t = t0
+                for i in range(n_req):
+                    t += gaps[i]
+                    d = t - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    tickets[i] = srv.submit(progs[keys[i]], params[i])
+            th = threading.Thread(target=producer)
+            th.start()
+            lat = {n: [] for n in sizes}
+            done_at = t0
+            for i in range(n_req):
+                while tickets[i] is None:
+                    time.sleep(0.0002)
+                _, _, info = srv.wait(tickets[i], timeout_s=600)
+                lat[keys[i][0]].append(info["total_us"] / 1000.0)
+                done_at = max(done_at, time.perf_counter())
+            th.join()
+            wall = done_at - t0
+            per = {str(n): {"count": len(v), "p50_ms": float(np.percentile(v, 50)) if v else None,
+                            "p99_ms": float(np.percentile(v, 99)) if v else None} for n, v in lat.items()}
+            results.append({"offered_req_s": lam, "requests": n_req, "throughput_req_s": n_req / wall,
+                            "per_qubits": per})
+        stats = srv.stats()
+    top = max(r["throughput_req_s"] for r in results)
+    line = {"metric": "serving value+grad requests/s (mixed n 4-24, HEA depth 2-12)", "value": top,
+            "unit": "requests/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64", "data": "synthetic",
+            "config": {"workload": "serving_stream_poisson", "rates_req_s": rates, "duration_s": a.duration,
+                       "qubits": sizes, "depth": [2, 12], "memory_budget_gb": a.budget_gb, "max_batch": 64},
+            "sweep": results, "server": stats}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -411,12 +479,18 @@ def main():
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
+    ap.add_argument("--workload", default="vqc", choices=["vqc", "serving"])
+    ap.add_argument("--rates", default="100,500,2000,5000")
+    ap.add_argument("--duration", type=float, default=2.0)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     a = ap.parse_args()
     if a.impl == "reference":
         return run_reference_arm(a)
+    if a.workload == "serving":
+        return run_serving(a)
     return run_ours(a)
 
 

@@ -108,7 +108,8 @@ typedef struct tedq_options {
   int32_t fuse;        /* 1: fused multi-gate passes; 0: one pass per gate (plain) */
   int32_t tile_qubits; /* 0 = default tile size (2^13 amplitudes for c64)          */
   int32_t jit;         /* specialised per-circuit pass kernels compiled with NVRTC:
-                          0 = auto (on for states of >= 14 qubits), 1 = on, -1 = off;
+                          0 = auto (on for states of >= 14 qubits), 1 = on, -1 = off,
+                          2 = on in the background (generic kernels until compiled);
                           the environment variable TEDQ_GB300_JIT=0 turns it off   */
   int32_t reserved[4];
 } tedq_options_t;
@@ -201,6 +202,64 @@ int32_t tedq_run_noalloc(tedq_program_t* prog, const void* params, int64_t batch
 int32_t tedq_run_adjoint(tedq_program_t* prog, const void* params, int64_t batch,
                          const void* dy_real, const void* dy_state, void* psi, void* lambda_,
                          void* grad, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- serving: continuous batching of circuit evaluations ----------------
+ * No counterpart in the reference (it evaluates one circuit per call; its
+ * QUDIO backend wraps torch.nn.DataParallel over a dataset,
+ * tedq/backends/qudio_backend.py:45-124).  A server owns one device-memory
+ * arena (the admission budget), a worker thread and a few streams.  Requests
+ * (program, parameters on the host, optional gradient) are queued; the worker
+ * groups queued requests of the same program into batches as capacity frees
+ * up, runs forward (+ adjoint) on its own streams while other batches are in
+ * flight, and completes each request when its batch's results are back on the
+ * host.  Requests that arrive while others run are admitted as soon as memory
+ * and stream slots allow. */
+typedef struct tedq_server tedq_server_t;
+
+typedef struct tedq_server_options {
+  int32_t device;              /* CUDA device index                                  */
+  int32_t n_streams;           /* concurrent batches (default 4)                     */
+  int32_t max_batch;           /* circuits per batch (default 256)                   */
+  int32_t max_wait_us;         /* batching window for a partially filled batch       */
+  int64_t memory_budget_bytes; /* device arena for states and buffers                */
+  int32_t paused;              /* 1: queue requests but launch nothing until
+                                  tedq_server_resume (deterministic batching)       */
+  int32_t pad;
+  int64_t reserved[3];
+} tedq_server_options_t;
+
+typedef struct tedq_request_result {
+  int32_t status;      /* TEDQ_OK or the failure status of the request             */
+  int32_t batch_size;  /* circuits in the batch that carried the request           */
+  double queue_us;     /* submit -> batch launch                                   */
+  double total_us;     /* submit -> results on the host                            */
+} tedq_request_result_t;
+
+typedef struct tedq_server_stats {
+  int64_t submitted, completed, failed, cancelled, batches;
+  int64_t in_flight_bytes, peak_in_flight_bytes;
+  int64_t reserved[4];
+} tedq_server_stats_t;
+
+int32_t tedq_server_create(const tedq_server_options_t* opts, tedq_server_t** out);
+/* Stops the worker after the batches in flight; queued requests fail with
+ * TEDQ_ERR_STATE. */
+int32_t tedq_server_destroy(tedq_server_t* server);
+/* params: host array of the program's n_params values (float for c64 programs,
+ * double for c128), copied at submission.  dy: host array of n_real_outputs
+ * cotangents or NULL for all ones; with_grad = 0 skips the adjoint. */
+int32_t tedq_server_submit(tedq_server_t* server, tedq_program_t* prog, const void* params,
+                           const void* dy, int32_t with_grad, int64_t* ticket);
+/* Waits at most timeout_us (< 0: no limit) for a request; copies its outputs
+ * (n_real_outputs) and gradient (n_params) into host arrays (either may be
+ * NULL).  TEDQ_ERR_TIMEOUT when the wait expires (the request stays valid);
+ * otherwise the request is released. */
+int32_t tedq_server_wait(tedq_server_t* server, int64_t ticket, int64_t timeout_us, void* out_real,
+                         void* grad, tedq_request_result_t* result);
+/* Cancels a request that has not been launched yet (TEDQ_ERR_STATE otherwise). */
+int32_t tedq_server_cancel(tedq_server_t* server, int64_t ticket);
+int32_t tedq_server_stats(tedq_server_t* server, tedq_server_stats_t* out);
+int32_t tedq_server_resume(tedq_server_t* server);
 
 /* ---- profiling -----------------------------------------------------------
  * When enabled, tedq_run / tedq_run_adjoint record a CUDA event pair on the

@@ -7,6 +7,7 @@
 // synchronisation.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -41,6 +42,7 @@ struct tedq_program {
   // specialised kernels: compiled in the background from program creation,
   // loaded per device on first use
   bool jit_on = false;
+  bool jit_background = false;  // use the generic kernels until compiled
   int jit_state = 0;  // 0 off, 1 compiling, 2 compiled, 3 loaded, -1 failed
   std::future<std::tuple<bool, std::vector<std::string>, std::string>> jit_future;
   std::vector<JitSource> jit_srcs;
@@ -81,8 +83,11 @@ cudaError_t timed(tedq_program* h, int family, int64_t amp_passes, cudaStream_t 
 }
 
 // Waits for the background compile; returns true when a cubin is available.
-bool jit_compiled(tedq_program* h) {
+bool jit_compiled(tedq_program* h, bool block = true) {
   if (!h->jit_on) return false;
+  if (h->jit_state == 1 && !block &&
+      h->jit_future.wait_for(std::chrono::seconds(0)) != std::future_status::ready)
+    return false;
   if (h->jit_state == 1) {
     auto r = h->jit_future.get();
     if (std::get<0>(r)) {
@@ -102,7 +107,7 @@ bool jit_compiled(tedq_program* h) {
 JitKernels* jit_kernels(tedq_program* h) {
   if (!h->jit_on) return nullptr;
   std::lock_guard<std::mutex> lock(h->jit_mu);
-  if (!jit_compiled(h)) return nullptr;
+  if (!jit_compiled(h, !h->jit_background)) return nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   if (!h->jit_tried[dev]) {
@@ -204,6 +209,7 @@ int32_t tedq_program_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
     const char* env = getenv("TEDQ_GB300_JIT");
     const int mode = opts ? opts->jit : 0;
     h->jit_on = mode > 0 || (mode == 0 && h->p->ns >= 14);
+    h->jit_background = mode == 2;
     if (env && env[0] == '0') h->jit_on = false;
     if (h->jit_on) {
       h->jit_state = 1;

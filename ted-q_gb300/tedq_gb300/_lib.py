@@ -63,6 +63,21 @@ class Profile(ctypes.Structure):
                 ("fwd_amp_passes", c_int64), ("bwd_amp_passes", c_int64), ("reserved", c_int64 * 4)]
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("device", c_int32), ("n_streams", c_int32), ("max_batch", c_int32), ("max_wait_us", c_int32),
+                ("memory_budget_bytes", c_int64), ("paused", c_int32), ("pad", c_int32), ("reserved", c_int64 * 3)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", c_int32), ("batch_size", c_int32), ("queue_us", c_double), ("total_us", c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_int64), ("completed", c_int64), ("failed", c_int64), ("cancelled", c_int64),
+                ("batches", c_int64), ("in_flight_bytes", c_int64), ("peak_in_flight_bytes", c_int64),
+                ("reserved", c_int64 * 4)]
+
+
 # every symbol the header declares, with (restype, argtypes)
 SIGNATURES = {
     "tedq_abi_version": (c_int32, []),
@@ -79,6 +94,13 @@ SIGNATURES = {
     "tedq_run_adjoint": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_size_t, c_void_p]),
     "tedq_run_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tedq_server_create": (c_int32, [POINTER(ServerOptions), POINTER(c_void_p)]),
+    "tedq_server_destroy": (c_int32, [c_void_p]),
+    "tedq_server_submit": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, POINTER(c_int64)]),
+    "tedq_server_wait": (c_int32, [c_void_p, c_int64, c_int64, c_void_p, c_void_p, POINTER(RequestResult)]),
+    "tedq_server_cancel": (c_int32, [c_void_p, c_int64]),
+    "tedq_server_stats": (c_int32, [c_void_p, POINTER(ServerStats)]),
+    "tedq_server_resume": (c_int32, [c_void_p]),
     "tedq_profile_enable": (c_int32, [c_void_p, c_int32]),
     "tedq_profile_read": (c_int32, [c_void_p, POINTER(Profile)]),
 }
