@@ -63,7 +63,11 @@ int32_t fail(int32_t status, const std::string& msg) {
 }
 
 int32_t cuda_fail(cudaError_t e, const char* where) {
-  return fail(TEDQ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+  std::string msg = std::string(where) + ": " + cudaGetErrorString(e);
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess && pending != e)
+    msg += std::string(" (earlier error pending in this thread: ") + cudaGetErrorString(pending) + ")";
+  return fail(TEDQ_ERR_CUDA, msg);
 }
 
 // Launch wrapper: with profiling on, brackets the launch with an event pair.

@@ -22,6 +22,10 @@
 // register work per amplitude is 4-8 FMA per gate.
 #include <cuda_runtime.h>
 
+#include <tuple>
+#include <type_traits>
+#include <utility>
+
 #include "sv_device.cuh"
 #include "sv_kernels.cuh"
 
@@ -407,6 +411,21 @@ __global__ void grad_finalize_kernel(const double* __restrict__ acc, real* __res
 
 // ---------------------------------------------------------------- launch helpers
 
+// Launches through cudaLaunchKernel so the status returned is the launch's own
+// (cudaGetLastError after <<<>>> also reports stale errors of earlier calls).
+template <typename... KArgs, size_t... I, typename Tup>
+cudaError_t launch_with(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Tup& t,
+                        std::index_sequence<I...>) {
+  void* ptrs[sizeof...(KArgs) > 0 ? sizeof...(KArgs) : 1] = {static_cast<void*>(&std::get<I>(t))...};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k), g, b, ptrs, smem, s);
+}
+
+template <typename... KArgs, typename... Actual>
+cudaError_t launch_kernel(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Actual&&... a) {
+  std::tuple<typename std::decay<KArgs>::type...> t(std::forward<Actual>(a)...);
+  return launch_with(k, g, b, smem, s, t, std::index_sequence_for<KArgs...>{});
+}
+
 constexpr int kMaxGridY = 65535;
 
 template <typename K>
@@ -434,9 +453,8 @@ cudaError_t fwd_impl(const PassParams& P, void* psi, const void* params, int n_p
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     dim3 grid(tiles, (unsigned)nb);
-    kern<<<grid, T, smem, s>>>(P, static_cast<cpx<real>*>(psi), static_cast<const real*>(params), n_params,
-                               static_cast<const cpx<real>*>(init), c0);
-    e = cudaGetLastError();
+    e = launch_kernel(kern, grid, dim3(T), smem, s, P, static_cast<cpx<real>*>(psi),
+                      static_cast<const real*>(params), n_params, static_cast<const cpx<real>*>(init), c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -455,9 +473,8 @@ cudaError_t bwd_impl(const PassParams& P, void* psi, void* lam, const void* para
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     dim3 grid(tiles, (unsigned)nb);
-    kern<<<grid, T, smem, s>>>(P, static_cast<cpx<real>*>(psi), static_cast<cpx<real>*>(lam),
-                               static_cast<const real*>(params), n_params, grad_acc, c0);
-    e = cudaGetLastError();
+    e = launch_kernel(kern, grid, dim3(T), smem, s, P, static_cast<cpx<real>*>(psi), static_cast<cpx<real>*>(lam),
+                      static_cast<const real*>(params), n_params, grad_acc, c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -469,9 +486,8 @@ cudaError_t init_impl(int n, int pad, void* psi, const void* init, int64_t batch
   const unsigned bx = (unsigned)((N + 255) / 256 < 4096 ? (N + 255) / 256 : 4096);
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    init_state_kernel<real><<<dim3(bx, (unsigned)nb), 256, 0, s>>>(static_cast<cpx<real>*>(psi), n, pad,
-                                                                   static_cast<const cpx<real>*>(init), c0);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_kernel(init_state_kernel<real>, dim3(bx, (unsigned)nb), dim3(256), 0, s,
+                                  static_cast<cpx<real>*>(psi), n, pad, static_cast<const cpx<real>*>(init), c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -483,9 +499,8 @@ cudaError_t expval_impl(int n, const TermTable& TT, const void* psi, double* acc
   const unsigned bx = (unsigned)((N + kMeasChunk - 1) / kMeasChunk);
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    expval_kernel<real><<<dim3(bx, (unsigned)nb), kMeasThreads, 0, s>>>(TT, static_cast<const cpx<real>*>(psi), n,
-                                                                         acc, c0);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_kernel(expval_kernel<real>, dim3(bx, (unsigned)nb), dim3(kMeasThreads), 0, s, TT,
+                                  static_cast<const cpx<real>*>(psi), n, acc, c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -505,9 +520,8 @@ cudaError_t probs_impl(int n, const ProbsTable& PT, const void* psi, double* pro
   if (e != cudaSuccess) return e;
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    kern<<<dim3(bx, (unsigned)nb), kMeasThreads, smem, s>>>(PT, static_cast<const cpx<real>*>(psi), n, probs_acc,
-                                                             static_cast<real*>(out), n_real, c0);
-    e = cudaGetLastError();
+    e = launch_kernel(kern, dim3(bx, (unsigned)nb), dim3(kMeasThreads), smem, s, PT,
+                      static_cast<const cpx<real>*>(psi), n, probs_acc, static_cast<real*>(out), n_real, c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -521,10 +535,9 @@ cudaError_t lambda_impl(int n, const TermTable& TT, const ProbsTable& PT, const 
   const unsigned bx = (unsigned)(chunks < 8192 ? chunks : 8192);
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    lambda_init_kernel<real><<<dim3(bx, (unsigned)nb), 256, 0, s>>>(
-        TT, PT, w, static_cast<const real*>(dy), n_real, static_cast<const cpx<real>*>(dys),
-        static_cast<const cpx<real>*>(psi), static_cast<cpx<real>*>(lam), n, c0);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_kernel(lambda_init_kernel<real>, dim3(bx, (unsigned)nb), dim3(256), 0, s, TT, PT, w,
+                                  static_cast<const real*>(dy), n_real, static_cast<const cpx<real>*>(dys),
+                                  static_cast<const cpx<real>*>(psi), static_cast<cpx<real>*>(lam), n, c0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -568,10 +581,10 @@ cudaError_t launch_finalize(bool dbl, const OutTermTable& O, const ProbsTable& P
   const int64_t total = batch * O.n_real;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (dbl)
-    finalize_kernel<double><<<blocks, 256, 0, s>>>(O, PT, term_acc, probs_acc, static_cast<double*>(out_real), batch);
-  else
-    finalize_kernel<float><<<blocks, 256, 0, s>>>(O, PT, term_acc, probs_acc, static_cast<float*>(out_real), batch);
-  return cudaGetLastError();
+    return launch_kernel(finalize_kernel<double>, dim3(blocks), dim3(256), 0, s, O, PT, term_acc, probs_acc,
+                         static_cast<double*>(out_real), batch);
+  return launch_kernel(finalize_kernel<float>, dim3(blocks), dim3(256), 0, s, O, PT, term_acc, probs_acc,
+                       static_cast<float*>(out_real), batch);
 }
 
 cudaError_t launch_term_weights(bool dbl, const OutTermTable& O, const void* dy_real, double* w, int64_t batch,
@@ -580,10 +593,10 @@ cudaError_t launch_term_weights(bool dbl, const OutTermTable& O, const void* dy_
   const int64_t total = batch * O.n_terms;
   const unsigned blocks = (unsigned)((total + 255) / 256);
   if (dbl)
-    term_weights_kernel<double><<<blocks, 256, 0, s>>>(O, static_cast<const double*>(dy_real), w, batch);
-  else
-    term_weights_kernel<float><<<blocks, 256, 0, s>>>(O, static_cast<const float*>(dy_real), w, batch);
-  return cudaGetLastError();
+    return launch_kernel(term_weights_kernel<double>, dim3(blocks), dim3(256), 0, s, O,
+                         static_cast<const double*>(dy_real), w, batch);
+  return launch_kernel(term_weights_kernel<float>, dim3(blocks), dim3(256), 0, s, O,
+                       static_cast<const float*>(dy_real), w, batch);
 }
 
 cudaError_t launch_lambda_init(bool dbl, int n, const TermTable& T, const ProbsTable& PT, const double* w,
@@ -596,9 +609,11 @@ cudaError_t launch_lambda_init(bool dbl, int n, const TermTable& T, const ProbsT
 cudaError_t launch_grad_finalize(bool dbl, const double* grad_acc, void* grad, int64_t count, cudaStream_t s) {
   if (count == 0) return cudaSuccess;
   const unsigned blocks = (unsigned)((count + 255) / 256);
-  if (dbl) grad_finalize_kernel<double><<<blocks, 256, 0, s>>>(grad_acc, static_cast<double*>(grad), count);
-  else grad_finalize_kernel<float><<<blocks, 256, 0, s>>>(grad_acc, static_cast<float*>(grad), count);
-  return cudaGetLastError();
+  if (dbl)
+    return launch_kernel(grad_finalize_kernel<double>, dim3(blocks), dim3(256), 0, s, grad_acc,
+                         static_cast<double*>(grad), count);
+  return launch_kernel(grad_finalize_kernel<float>, dim3(blocks), dim3(256), 0, s, grad_acc,
+                       static_cast<float*>(grad), count);
 }
 
 }  // namespace tedq
