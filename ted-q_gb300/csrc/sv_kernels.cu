@@ -22,6 +22,7 @@
 // register work per amplitude is 4-8 FMA per gate.
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <tuple>
 #include <type_traits>
 #include <utility>
@@ -428,15 +429,21 @@ cudaError_t launch_kernel(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cuda
 
 constexpr int kMaxGridY = 65535;
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`.  The limit
+// is a property of the function (shared by all host threads), so the record of
+// what was set is process-wide per device and the limit is never lowered.
 template <typename K>
 cudaError_t ensure_smem(K kernel, size_t bytes) {
+  static std::mutex mu;
+  static size_t done_bytes[64] = {0};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  static thread_local size_t done_bytes[64] = {0};
-  if (dev < 64 && done_bytes[dev] >= bytes) return cudaSuccess;
+  if (dev < 0 || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done_bytes[dev] >= bytes) return cudaSuccess;
   e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess && dev < 64) done_bytes[dev] = bytes;
+  if (e == cudaSuccess) done_bytes[dev] = bytes;
   return e;
 }
 

@@ -102,3 +102,17 @@ def test_submit_wrong_parameter_count():
     with Server(memory_budget_bytes=16 << 20) as srv:
         with pytest.raises(ValueError):
             srv.submit(cc, np.zeros(cc.num_params + 1, dtype=np.float32))
+
+
+def test_kernel_limits_shared_across_threads():
+    """A small circuit run on another host thread must not lower the shared-
+    memory limit a larger circuit needs on this thread."""
+    big = _compile(13, 1)
+    small = _compile(4, 1)
+    big.execute_batch(torch.zeros(1, big.num_params, device=DEV))
+    th = threading.Thread(target=lambda: small.execute_batch(torch.zeros(1, small.num_params, device=DEV)))
+    th.start()
+    th.join()
+    out = big.execute_batch(torch.zeros(2, big.num_params, device=DEV))
+    torch.cuda.synchronize()
+    assert torch.allclose(out, torch.ones_like(out))
