@@ -280,6 +280,69 @@ typedef struct tedq_profile {
 int32_t tedq_profile_enable(tedq_program_t* prog, int32_t on);
 int32_t tedq_profile_read(tedq_program_t* prog, tedq_profile_t* out);
 
+/* ---- tensor-network mode --------------------------------------------------
+ * Replaces the TN branch of PyTorchBackend.execute (pytorch_backend.py:242-356):
+ * the sandwich network of gen_tensor_networks (tensor_network.py:850-1099),
+ * the external path optimiser (OEWrapper, oe_wrapper.py:24-65; JDOptTN,
+ * compiled_circuit.py:388-393) and torch einsum.  One network per
+ * measurement, reduced to the backward light cone of its observable, ordered
+ * by randomised greedy search and sliced until every intermediate fits
+ * 2^max_rank entries.  Each pairwise contraction runs as two bit-permutation
+ * gathers into planar real operands and one real GEMM on the tensor cores
+ * (4M decomposition: [Re A; Im A] x [Re B, Im B]), batched over the circuits
+ * of a call.  Expectation values of tensor products of observable factors
+ * only (the reference's TN mode also returns probs/state, :1017-1022). */
+typedef struct tedq_tn_plan tedq_tn_plan_t;
+
+/* GEMM arithmetic of the complex64 mode (complex128 uses FP64 GEMMs). */
+enum {
+  TEDQ_TN_GEMM_BF16X9 = 0,  /* FP32 accuracy from BF16 tensor-core products
+                               (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9)    */
+  TEDQ_TN_GEMM_TF32 = 1,    /* one TF32 product per term (~1e-3 relative)     */
+  TEDQ_TN_GEMM_FP32 = 2     /* FP32 without tensor cores                      */
+};
+
+typedef struct tedq_tn_options {
+  int32_t precision;   /* TEDQ_PREC_C64 / TEDQ_PREC_C128                       */
+  int32_t gemm;        /* TEDQ_TN_GEMM_* (complex64 only)                      */
+  int32_t max_rank;    /* 0 = 27                                               */
+  int32_t repeats;     /* randomised greedy trials, 0 = 64                     */
+  uint64_t seed;       /* 0 = 1                                                */
+  int32_t graphs;      /* 1: replay each call's launches as a CUDA graph       */
+  int32_t reserved[3];
+} tedq_tn_options_t;
+
+typedef struct tedq_tn_info {
+  int32_t n_qubits;
+  int32_t n_params;
+  int32_t n_meas;
+  int32_t n_steps;          /* pairwise contractions, all measurements         */
+  int32_t max_rank;         /* largest intermediate: 2^max_rank entries         */
+  int32_t n_sliced;         /* sliced indices (largest over measurements)      */
+  int32_t gates_kept;       /* circuit gates inside the light cones (sum)      */
+  int32_t precision;
+  double log2_flops;        /* log2 of real flops per circuit (8 per complex MAC) */
+  int64_t workspace_per_circuit;
+  int64_t workspace_fixed;  /* bytes independent of the batch                  */
+  int64_t reserved[4];
+} tedq_tn_info_t;
+
+int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n_qubits,
+                            const tedq_meas_t* meas, int32_t n_meas, const tedq_tn_options_t* opts,
+                            tedq_tn_plan_t** out);
+int32_t tedq_tn_plan_destroy(tedq_tn_plan_t* plan);
+int32_t tedq_tn_plan_info(const tedq_tn_plan_t* plan, tedq_tn_info_t* info);
+/* JSON export of the networks, orders, gather tables and layouts; returns the
+ * length needed including the terminating zero (-1 on error). */
+int64_t tedq_tn_plan_describe(const tedq_tn_plan_t* plan, char* buf, int64_t len);
+/* Device workspace (bytes) of tedq_tn_contract for a batch (-1 on error). */
+int64_t tedq_tn_workspace_bytes(const tedq_tn_plan_t* plan, int64_t batch);
+/* params    [batch][n_params] float (c64) / double (c128), device
+ * out       [batch][n_meas]   float / double, device
+ * workspace >= tedq_tn_workspace_bytes(batch) bytes, device, 256-byte aligned */
+int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch, void* out,
+                         void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

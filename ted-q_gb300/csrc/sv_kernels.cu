@@ -29,6 +29,7 @@
 
 #include "sv_device.cuh"
 #include "sv_kernels.cuh"
+#include "launch.cuh"
 
 namespace tedq {
 namespace {
@@ -411,21 +412,6 @@ __global__ void grad_finalize_kernel(const double* __restrict__ acc, real* __res
 }
 
 // ---------------------------------------------------------------- launch helpers
-
-// Launches through cudaLaunchKernel so the status returned is the launch's own
-// (cudaGetLastError after <<<>>> also reports stale errors of earlier calls).
-template <typename... KArgs, size_t... I, typename Tup>
-cudaError_t launch_with(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Tup& t,
-                        std::index_sequence<I...>) {
-  void* ptrs[sizeof...(KArgs) > 0 ? sizeof...(KArgs) : 1] = {static_cast<void*>(&std::get<I>(t))...};
-  return cudaLaunchKernel(reinterpret_cast<const void*>(k), g, b, ptrs, smem, s);
-}
-
-template <typename... KArgs, typename... Actual>
-cudaError_t launch_kernel(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, Actual&&... a) {
-  std::tuple<typename std::decay<KArgs>::type...> t(std::forward<Actual>(a)...);
-  return launch_with(k, g, b, smem, s, t, std::index_sequence_for<KArgs...>{});
-}
 
 constexpr int kMaxGridY = 65535;
 

@@ -1,0 +1,510 @@
+// tn_capi.cpp -- extern "C" entry points of the tensor-network mode
+// (include/tedq_gb300.h, "tensor-network mode").
+//
+// Reference counterpart: the TN branch of PyTorchBackend.execute
+// (tedq/backends/pytorch_backend.py:242-356), which rebuilds the operand list
+// per call (compiled_circuit.py:442-467, pytorch_backend.py:524-546) and hands
+// it to the path object's contract().  Here the plan is built once; a call
+// builds the parameter-dependent gate tensors of the whole batch on the device
+// and runs the planned pairwise contractions, each as one gather launch and
+// one strided-batched real GEMM over the batch.  cuBLAS is opened at run time
+// (no link-time dependency), and a CUDA graph of a call's launches can be
+// replayed when the same buffers are used again.
+#include <cuda_runtime.h>
+#include <cublas_api.h>  // types and enums; the library is opened with dlopen
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sv_program.h"
+#include "tedq_gb300.h"
+#include "tn_kernels.cuh"
+#include "tn_plan.h"
+
+using namespace tedq;
+
+int32_t tedq_record_error(int32_t status, const char* msg);
+
+namespace {
+
+// ------------------------------------------------------------------ cuBLAS
+
+struct Blas {
+  bool ok = false;
+  std::string why;
+  cublasStatus_t (*create)(cublasHandle_t*) = nullptr;
+  cublasStatus_t (*destroy)(cublasHandle_t) = nullptr;
+  cublasStatus_t (*set_stream)(cublasHandle_t, cudaStream_t) = nullptr;
+  cublasStatus_t (*set_workspace)(cublasHandle_t, void*, size_t) = nullptr;
+  cublasStatus_t (*set_emulation)(cublasHandle_t, cublasEmulationStrategy_t) = nullptr;
+  const char* (*status_string)(cublasStatus_t) = nullptr;
+  cublasStatus_t (*gemm)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int, int, int, const void*,
+                         const void*, cudaDataType, int, long long, const void*, cudaDataType, int, long long,
+                         const void*, void*, cudaDataType, int, long long, int, cublasComputeType_t,
+                         cublasGemmAlgo_t) = nullptr;
+};
+
+Blas load_blas() {
+  Blas b;
+  std::vector<std::string> cands = {"libcublas.so.13", "libcublas.so"};
+  for (const char* env : {"CUDA_HOME", "CUDA_PATH"})
+    if (const char* d = getenv(env)) cands.push_back(std::string(d) + "/lib64/libcublas.so.13");
+  cands.push_back("/usr/local/cuda/lib64/libcublas.so.13");
+  void* h = nullptr;
+  for (auto& c : cands)
+    if ((h = dlopen(c.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) {
+    b.why = "libcublas.so.13 not found";
+    return b;
+  }
+#define TEDQ_SYM(field, name)                                  \
+  b.field = reinterpret_cast<decltype(b.field)>(dlsym(h, name)); \
+  if (!b.field) {                                              \
+    b.why = std::string("missing symbol ") + name;             \
+    return b;                                                  \
+  }
+  TEDQ_SYM(create, "cublasCreate_v2")
+  TEDQ_SYM(destroy, "cublasDestroy_v2")
+  TEDQ_SYM(set_stream, "cublasSetStream_v2")
+  TEDQ_SYM(set_workspace, "cublasSetWorkspace_v2")
+  TEDQ_SYM(set_emulation, "cublasSetEmulationStrategy")
+  TEDQ_SYM(status_string, "cublasGetStatusString")
+  TEDQ_SYM(gemm, "cublasGemmStridedBatchedEx")
+#undef TEDQ_SYM
+  b.ok = true;
+  return b;
+}
+
+Blas& blas() {
+  static Blas b = load_blas();
+  return b;
+}
+
+constexpr size_t kBlasWorkspace = 32ull << 20;
+
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------- plan
+
+struct TnDevice {
+  bool ready = false;
+  cublasHandle_t handle = nullptr;
+  void* consts = nullptr;       // constants of all networks (plan precision)
+  TnLeafDesc* desc = nullptr;   // batched-leaf descriptors of all networks
+  // graph of the last call, replayed while its arguments repeat
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+  const void* g_params = nullptr;
+  void* g_out = nullptr;
+  void* g_ws = nullptr;
+  int64_t g_batch = -1;
+};
+
+struct tedq_tn_plan {
+  std::vector<TnNet> nets;
+  int n = 0, n_params = 0, precision = TEDQ_PREC_C64, gemm = TEDQ_TN_GEMM_BF16X9;
+  bool graphs = false;
+  std::vector<std::vector<TnLeafDesc>> descs;
+  std::vector<int64_t> const_base;  // reals, per network
+  std::vector<int64_t> desc_base;   // descriptors, per network
+  int64_t const_total = 0, desc_total = 0;
+  std::mutex mu;
+  TnDevice dev[64];
+};
+
+namespace {
+
+int64_t elem_bytes(const tedq_tn_plan* p) { return p->precision == TEDQ_PREC_C128 ? 8 : 4; }
+
+struct Layout {
+  size_t acc, blas_ws, leaves, arena_b, arena_u, scratch, total;
+};
+
+// acc (FP64 sums) | cuBLAS workspace | per network (reused): batched leaves,
+// batched arena, unbatched arena, GEMM operand scratch
+Layout layout(const tedq_tn_plan* p, int64_t batch) {
+  const size_t es = (size_t)elem_bytes(p);
+  Layout L{};
+  L.acc = 0;
+  L.blas_ws = align256((size_t)batch * p->nets.size() * sizeof(double));
+  size_t region = L.blas_ws + kBlasWorkspace;
+  size_t most = 0, mleaves = 0, mab = 0, mau = 0;
+  for (const TnNet& n : p->nets) {
+    size_t lv = align256(2 * (size_t)n.batched_leaf_elems * batch * es);
+    size_t ab = align256((size_t)n.batched_arena * batch * es);
+    size_t au = align256((size_t)n.unbatched_arena * es);
+    size_t sc = align256((size_t)tn_scratch_reals(n, batch) * es);
+    mleaves = std::max(mleaves, lv);
+    mab = std::max(mab, ab);
+    mau = std::max(mau, au);
+    most = std::max(most, sc);
+  }
+  L.leaves = region;
+  L.arena_b = L.leaves + mleaves;
+  L.arena_u = L.arena_b + mab;
+  L.scratch = L.arena_u + mau;
+  L.total = L.scratch + most;
+  return L;
+}
+
+int32_t fail(int32_t status, const std::string& msg) { return tedq_record_error(status, msg.c_str()); }
+
+int32_t cuda_fail(const char* where, cudaError_t e) {
+  return fail(TEDQ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int32_t blas_fail(const char* where, cublasStatus_t st) {
+  return fail(TEDQ_ERR_CUDA, std::string(where) + ": " + blas().status_string(st));
+}
+
+#define TEDQ_CUDA(where, expr)                    \
+  do {                                            \
+    cudaError_t e_ = (expr);                      \
+    if (e_ != cudaSuccess) return cuda_fail(where, e_); \
+  } while (0)
+
+// Device-resident constants, descriptors and the cuBLAS handle (first use).
+int32_t ensure_device(tedq_tn_plan* p, int dev) {
+  TnDevice& D = p->dev[dev];
+  if (D.ready) return TEDQ_OK;
+  Blas& B = blas();
+  if (!B.ok) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: cuBLAS unavailable: " + B.why);
+  if (!D.handle) {
+    cublasStatus_t st = B.create(&D.handle);
+    if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasCreate", st);
+    if (p->precision == TEDQ_PREC_C64 && p->gemm == TEDQ_TN_GEMM_BF16X9) {
+      st = B.set_emulation(D.handle, CUBLAS_EMULATION_STRATEGY_EAGER);
+      if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetEmulationStrategy", st);
+    }
+  }
+  const size_t es = (size_t)elem_bytes(p);
+  if (!D.consts) {
+    std::vector<char> host(std::max<int64_t>(p->const_total, 1) * es);
+    int64_t k = 0;
+    for (const TnNet& n : p->nets)
+      for (double v : n.constants) {
+        if (es == 8) reinterpret_cast<double*>(host.data())[k++] = v;
+        else reinterpret_cast<float*>(host.data())[k++] = (float)v;
+      }
+    TEDQ_CUDA("tedq_tn_contract: cudaMalloc", cudaMalloc(&D.consts, host.size()));
+    TEDQ_CUDA("tedq_tn_contract: cudaMemcpy", cudaMemcpy(D.consts, host.data(), host.size(), cudaMemcpyHostToDevice));
+  }
+  if (!D.desc && p->desc_total) {
+    std::vector<TnLeafDesc> all;
+    for (auto& d : p->descs) all.insert(all.end(), d.begin(), d.end());
+    TEDQ_CUDA("tedq_tn_contract: cudaMalloc", cudaMalloc(&D.desc, all.size() * sizeof(TnLeafDesc)));
+    TEDQ_CUDA("tedq_tn_contract: cudaMemcpy",
+              cudaMemcpy(D.desc, all.data(), all.size() * sizeof(TnLeafDesc), cudaMemcpyHostToDevice));
+  }
+  if (p->graphs && !D.capture)
+    TEDQ_CUDA("tedq_tn_contract: cudaStreamCreate", cudaStreamCreateWithFlags(&D.capture, cudaStreamNonBlocking));
+  D.ready = true;
+  return TEDQ_OK;
+}
+
+// Enqueues one call: batched gate tensors, then per network and slice the
+// gathers and GEMMs of every step and the FP64 root accumulation.
+template <typename real>
+int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch, real* out, char* ws,
+                cudaStream_t s) {
+  const Layout L = layout(p, batch);
+  Blas& bl = blas();
+  cublasStatus_t st = bl.set_stream(D.handle, s);
+  if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetStream", st);
+  st = bl.set_workspace(D.handle, ws + L.blas_ws, kBlasWorkspace);
+  if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetWorkspace", st);
+  double* acc = reinterpret_cast<double*>(ws + L.acc);
+  real* leaves = reinterpret_cast<real*>(ws + L.leaves);
+  real* arena_b = reinterpret_cast<real*>(ws + L.arena_b);
+  real* arena_u = reinterpret_cast<real*>(ws + L.arena_u);
+  real* scratch = reinterpret_cast<real*>(ws + L.scratch);
+  const bool dbl = sizeof(real) == 8;
+  const cudaDataType dt = dbl ? CUDA_R_64F : CUDA_R_32F;
+  cublasComputeType_t ct = CUBLAS_COMPUTE_64F;
+  if (!dbl)
+    ct = p->gemm == TEDQ_TN_GEMM_TF32   ? CUBLAS_COMPUTE_32F_FAST_TF32
+         : p->gemm == TEDQ_TN_GEMM_FP32 ? CUBLAS_COMPUTE_32F
+                                        : CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+  const real one = 1, zero = 0;
+  const int n_meas = (int)p->nets.size();
+  for (int m = 0; m < n_meas; ++m) {
+    const TnNet& net = p->nets[m];
+    const real* consts = static_cast<const real*>(D.consts) + p->const_base[m];
+    if (!p->descs[m].empty())
+      TEDQ_CUDA("tedq_tn_contract: leaf kernel",
+                tn_build_leaves<real>(D.desc + p->desc_base[m], (int)p->descs[m].size(), params, p->n_params,
+                                      batch, leaves, s));
+    auto source = [&](int t, TnGatherOp& o) {
+      const TnTensor& T = net.tensors[t];
+      if (T.leaf >= 0) {
+        o.kind = 0;
+        o.lm = o.ln = 0;
+        o.src = T.batched ? leaves + 2 * T.off * batch : consts + 2 * T.off;
+        o.src_bstride = T.batched ? (2ll << T.full_idx.size()) : 0;
+      } else {
+        o.kind = 1;
+        o.lm = T.lm;
+        o.ln = T.ln;
+        o.src = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
+        o.src_bstride = T.batched ? (4ll << (T.lm + T.ln)) : 0;
+      }
+    };
+    const int64_t n_slices = 1ll << net.sliced.size();
+    for (int64_t sl = 0; sl < n_slices; ++sl) {
+      for (const TnStep& stp : net.steps) {
+        TnGatherArgs A;
+        std::memset(&A, 0, sizeof(A));
+        const TnOperand* ops[2] = {&stp.opa, &stp.opb};
+        for (int x = 0; x < 2; ++x) {
+          const TnOperand& op = *ops[x];
+          TnGatherOp& o = A.op[x];
+          source(op.tensor, o);
+          o.nbits = op.nf + op.nc;
+          if (o.nbits > kTnMaxBits) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
+          for (int j = 0; j < o.nbits; ++j) o.bit[j] = (int8_t)op.src_bit[j];
+          o.base = 0;
+          for (auto& qb : op.slice_bit) o.base += ((sl >> qb.first) & 1) << qb.second;
+          o.nb = net.tensors[op.tensor].batched ? batch : 1;
+        }
+        A.op[0].dst = scratch;
+        A.op[1].dst = scratch + (2ll << A.op[0].nbits) * A.op[0].nb;
+        TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_gather<real>(A, s));
+        const TnTensor& T = net.tensors[stp.out];
+        const long long M = 1ll << stp.opa.nf, N = 1ll << stp.opb.nf, K = 1ll << stp.opa.nc;
+        real* C = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
+        st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)(2 * M), (int)(2 * N), (int)K, &one, A.op[0].dst, dt,
+                     (int)K, A.op[0].nb > 1 ? 2 * M * K : 0, A.op[1].dst, dt, (int)K, A.op[1].nb > 1 ? 2 * N * K : 0,
+                     &zero, C, dt, (int)(2 * M), 4 * M * N, stp.batched ? (int)batch : 1, ct, CUBLAS_GEMM_DEFAULT);
+        if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
+      }
+      const TnTensor& R = net.tensors[net.root];
+      const real* root = R.batched ? arena_b + R.arena * batch : arena_u + R.arena;
+      TEDQ_CUDA("tedq_tn_contract: root kernel",
+                tn_root<real>(root, R.batched ? 4 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
+    }
+  }
+  return TEDQ_OK;
+}
+
+template <typename real>
+int32_t contract(tedq_tn_plan* p, TnDevice& D, const void* params, int64_t batch, void* out, char* ws,
+                 cudaStream_t s) {
+  const real* prm = static_cast<const real*>(params);
+  real* o = static_cast<real*>(out);
+  if (!p->graphs) return enqueue<real>(p, D, prm, batch, o, ws, s);
+  const bool same = D.g_params == params && D.g_out == out && D.g_ws == ws && D.g_batch == batch;
+  if (!same) {
+    // new arguments: run eagerly, capture on the next call with the same ones
+    if (D.exec) cudaGraphExecDestroy(D.exec);
+    D.exec = nullptr;
+    D.g_params = params;
+    D.g_out = out;
+    D.g_ws = ws;
+    D.g_batch = batch;
+    return enqueue<real>(p, D, prm, batch, o, ws, s);
+  }
+  if (!D.exec) {
+    cudaGraph_t g = nullptr;
+    TEDQ_CUDA("tedq_tn_contract: cudaStreamBeginCapture",
+              cudaStreamBeginCapture(D.capture, cudaStreamCaptureModeThreadLocal));
+    int32_t rc = enqueue<real>(p, D, prm, batch, o, ws, D.capture);
+    cudaError_t e = cudaStreamEndCapture(D.capture, &g);
+    if (rc != TEDQ_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail("tedq_tn_contract: cudaStreamEndCapture", e);
+    e = cudaGraphInstantiate(&D.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      D.exec = nullptr;
+      return cuda_fail("tedq_tn_contract: cudaGraphInstantiate", e);
+    }
+  }
+  TEDQ_CUDA("tedq_tn_contract: cudaGraphLaunch", cudaGraphLaunch(D.exec, s));
+  return TEDQ_OK;
+}
+
+void release_devices(tedq_tn_plan* p) {
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (int d = 0; d < 64; ++d) {
+    TnDevice& D = p->dev[d];
+    if (!D.handle && !D.consts && !D.desc && !D.exec && !D.capture) continue;
+    cudaSetDevice(d);
+    if (D.exec) cudaGraphExecDestroy(D.exec);
+    if (D.capture) cudaStreamDestroy(D.capture);
+    if (D.consts) cudaFree(D.consts);
+    if (D.desc) cudaFree(D.desc);
+    if (D.handle) blas().destroy(D.handle);
+    D = TnDevice();
+  }
+  cudaSetDevice(cur);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n_qubits, const tedq_meas_t* meas,
+                            int32_t n_meas, const tedq_tn_options_t* opts, tedq_tn_plan_t** out) {
+  if (!out) return fail(TEDQ_ERR_ARG, "tedq_tn_plan_create: out is null");
+  *out = nullptr;
+  if (n_meas < 1 || !meas) return fail(TEDQ_ERR_ARG, "tedq_tn_plan_create: no measurements");
+  tedq_tn_plan* p = nullptr;
+  try {
+    p = new tedq_tn_plan();
+    TnPlanOptions po;
+    if (opts) {
+      if (opts->precision != TEDQ_PREC_C64 && opts->precision != TEDQ_PREC_C128)
+        throw std::invalid_argument("unknown precision");
+      if (opts->gemm < TEDQ_TN_GEMM_BF16X9 || opts->gemm > TEDQ_TN_GEMM_FP32)
+        throw std::invalid_argument("unknown GEMM mode");
+      if (opts->max_rank < 0 || opts->max_rank > 34) throw std::invalid_argument("max_rank out of range");
+      p->precision = opts->precision;
+      p->gemm = opts->gemm;
+      p->graphs = opts->graphs != 0;
+      if (opts->max_rank) po.max_rank = opts->max_rank;
+      if (opts->repeats > 0) po.repeats = opts->repeats;
+      if (opts->seed) po.seed = opts->seed;
+    }
+    p->n = n_qubits;
+    for (int i = 0; i < n_gates && gates; ++i)
+      for (int j = 0; j < 3; ++j) p->n_params = std::max(p->n_params, gates[i].param_slot[j] + 1);
+    for (int m = 0; m < n_meas; ++m) {
+      p->nets.push_back(tn_build(gates, n_gates, n_qubits, meas[m], po));
+      const TnNet& net = p->nets.back();
+      std::vector<TnLeafDesc> d;
+      for (int t = 0; t < net.n_leaves; ++t) {
+        const TnTensor& T = net.tensors[t];
+        if (!T.batched) continue;
+        const TnGate& g = net.gates[T.gate];
+        TnLeafDesc x;
+        std::memset(&x, 0, sizeof(x));
+        x.op = g.op;
+        x.k = g.k;
+        x.conj = T.leaf == TL_GATE_CONJ;
+        for (int j = 0; j < 3; ++j) {
+          x.slot[j] = g.slot[j];
+          x.val[j] = g.val[j];
+        }
+        x.slot[3] = -1;
+        x.off = T.off;
+        d.push_back(x);
+      }
+      p->const_base.push_back(p->const_total);
+      p->const_total += (int64_t)net.constants.size();
+      p->desc_base.push_back(p->desc_total);
+      p->desc_total += (int64_t)d.size();
+      p->descs.push_back(std::move(d));
+    }
+    *out = p;
+    return TEDQ_OK;
+  } catch (const UnsupportedError& e) {
+    delete p;
+    return fail(TEDQ_ERR_UNSUPPORTED, std::string("tedq_tn_plan_create: ") + e.what());
+  } catch (const std::bad_alloc&) {
+    delete p;
+    return fail(TEDQ_ERR_OOM, "tedq_tn_plan_create: out of host memory");
+  } catch (const std::exception& e) {
+    delete p;
+    return fail(TEDQ_ERR_ARG, std::string("tedq_tn_plan_create: ") + e.what());
+  }
+}
+
+int32_t tedq_tn_plan_destroy(tedq_tn_plan_t* plan) {
+  if (!plan) return TEDQ_OK;
+  release_devices(plan);
+  delete plan;
+  return TEDQ_OK;
+}
+
+int32_t tedq_tn_plan_info(const tedq_tn_plan_t* plan, tedq_tn_info_t* info) {
+  if (!plan || !info) return fail(TEDQ_ERR_ARG, "tedq_tn_plan_info: null argument");
+  std::memset(info, 0, sizeof(*info));
+  info->n_qubits = plan->n;
+  info->n_params = plan->n_params;
+  info->n_meas = (int32_t)plan->nets.size();
+  info->precision = plan->precision;
+  double flops = 0;
+  for (const TnNet& n : plan->nets) {
+    info->n_steps += (int32_t)n.steps.size();
+    info->max_rank = std::max(info->max_rank, n.max_rank);
+    info->n_sliced = std::max(info->n_sliced, (int32_t)n.sliced.size());
+    info->gates_kept += n.gates_kept;
+    flops += std::exp2(n.log2_flops);
+  }
+  info->log2_flops = std::log2(flops);
+  const Layout L1 = layout(plan, 1), L2 = layout(plan, 2);
+  info->workspace_per_circuit = (int64_t)(L2.total - L1.total);
+  info->workspace_fixed = (int64_t)L1.total - info->workspace_per_circuit;
+  return TEDQ_OK;
+}
+
+int64_t tedq_tn_plan_describe(const tedq_tn_plan_t* plan, char* buf, int64_t len) {
+  if (!plan) {
+    fail(TEDQ_ERR_ARG, "tedq_tn_plan_describe: plan is null");
+    return -1;
+  }
+  try {
+    std::string s = tn_describe(plan->nets, plan->n_params, plan->precision);
+    if (buf && len > 0) {
+      int64_t k = std::min<int64_t>((int64_t)s.size(), len - 1);
+      std::memcpy(buf, s.data(), (size_t)k);
+      buf[k] = 0;
+    }
+    return (int64_t)s.size() + 1;
+  } catch (const std::exception& e) {
+    fail(TEDQ_ERR_OOM, std::string("tedq_tn_plan_describe: ") + e.what());
+    return -1;
+  }
+}
+
+int64_t tedq_tn_workspace_bytes(const tedq_tn_plan_t* plan, int64_t batch) {
+  if (!plan || batch < 1) {
+    fail(TEDQ_ERR_ARG, "tedq_tn_workspace_bytes: invalid argument");
+    return -1;
+  }
+  return (int64_t)layout(plan, batch).total;
+}
+
+int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch, void* out, void* workspace,
+                         size_t workspace_bytes, void* stream) {
+  if (!plan) return fail(TEDQ_ERR_ARG, "tedq_tn_contract: plan is null");
+  if (batch < 1 || batch > (1ll << 30)) return fail(TEDQ_ERR_ARG, "tedq_tn_contract: batch out of range");
+  if (plan->n_params > 0 && !params) return fail(TEDQ_ERR_ARG, "tedq_tn_contract: params is null");
+  if (!out || !workspace) return fail(TEDQ_ERR_ARG, "tedq_tn_contract: out or workspace is null");
+  if (reinterpret_cast<uintptr_t>(workspace) & 255)
+    return fail(TEDQ_ERR_ARG, "tedq_tn_contract: workspace is not 256-byte aligned");
+  const Layout L = layout(plan, batch);
+  if (workspace_bytes < L.total)
+    return fail(TEDQ_ERR_ARG, "tedq_tn_contract: workspace too small (" + std::to_string(L.total) + " bytes needed)");
+  try {
+    int dev = 0;
+    TEDQ_CUDA("tedq_tn_contract: cudaGetDevice", cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: device index above 63");
+    std::lock_guard<std::mutex> lk(plan->mu);
+    int32_t rc = ensure_device(plan, dev);
+    if (rc != TEDQ_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    return plan->precision == TEDQ_PREC_C128
+               ? contract<double>(plan, plan->dev[dev], params, batch, out, ws, s)
+               : contract<float>(plan, plan->dev[dev], params, batch, out, ws, s);
+  } catch (const std::bad_alloc&) {
+    return fail(TEDQ_ERR_OOM, "tedq_tn_contract: out of host memory");
+  } catch (const std::exception& e) {
+    return fail(TEDQ_ERR_ARG, std::string("tedq_tn_contract: ") + e.what());
+  }
+}
+
+}  // extern "C"

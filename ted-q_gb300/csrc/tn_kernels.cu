@@ -1,0 +1,180 @@
+// tn_kernels.cu -- kernels of the tensor-network mode (tn_kernels.cuh).
+//
+// Work per pairwise contraction of A (M x K) and B (K x N), complex:
+//  * one gather launch writes both planar real operands [Re A; Im A] (2M x K,
+//    K contiguous) and [Re B, Im B] (K contiguous per column): a bit
+//    permutation of the source index, fused with the complex combination of
+//    the producer's real product when the source is an intermediate;
+//  * one real GEMM (2M x 2N x K) on the tensor cores (cuBLAS), whose four
+//    blocks are ArBr, ArBi, AiBr, AiBi -- the 4M real decomposition; the
+//    complex result is formed by whichever gather reads it next.
+// Gather traffic per operand entry: 8 B read from a leaf or 16 B from a real
+// product (c64), 8 B written.
+#include <cuda_runtime.h>
+
+#include "launch.cuh"
+#include "tedq_gb300.h"
+#include "tn_kernels.cuh"
+
+namespace tedq {
+namespace {
+
+__device__ __forceinline__ void sc(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sc(double x, double* s, double* c) { sincos(x, s, c); }
+
+// Row-major 2x2 of a parameterised one-qubit rotation, (re, im) pairs.
+// Definitions: tedq/QInterpreter/operators/qubit.py (RX :990-997,
+// RY :1048-1055, RZ :1106-1112, Rot :1169-1189, PhaseShift :1253-1257).
+template <typename real>
+__device__ void rot_2x2(int op, const real* a, real* m) {
+  real s, c;
+  for (int i = 0; i < 8; ++i) m[i] = 0;
+  switch (op) {
+    case TEDQ_OP_RX: case TEDQ_OP_CRX:
+      sc(a[0] / 2, &s, &c);
+      m[0] = c; m[3] = -s; m[5] = -s; m[6] = c;
+      break;
+    case TEDQ_OP_RY: case TEDQ_OP_CRY:
+      sc(a[0] / 2, &s, &c);
+      m[0] = c; m[2] = -s; m[4] = s; m[6] = c;
+      break;
+    case TEDQ_OP_RZ: case TEDQ_OP_CRZ:
+      sc(a[0] / 2, &s, &c);
+      m[0] = c; m[1] = -s; m[6] = c; m[7] = s;
+      break;
+    case TEDQ_OP_PHASESHIFT: case TEDQ_OP_CPHASE:
+      sc(a[0], &s, &c);
+      m[0] = 1; m[6] = c; m[7] = s;
+      break;
+    default: {  // Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi)
+      real sp, cp, sm, cm;
+      sc(a[1] / 2, &s, &c);
+      sc((a[0] + a[2]) / 2, &sp, &cp);
+      sc((a[0] - a[2]) / 2, &sm, &cm);
+      m[0] = cp * c; m[1] = -sp * c;
+      m[2] = -cm * s; m[3] = -sm * s;
+      m[4] = cm * s; m[5] = -sm * s;
+      m[6] = cp * c; m[7] = sp * c;
+      break;
+    }
+  }
+}
+
+// One thread per (tensor, circuit): consecutive threads write consecutive
+// circuits of one tensor (contiguous 4^k-entry blocks).
+template <typename real>
+__global__ void __launch_bounds__(256) tn_leaf_kernel(const TnLeafDesc* __restrict__ desc, int n_desc,
+                                                      const real* __restrict__ prm, int n_params,
+                                                      int64_t batch, real* __restrict__ leaves) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n_desc * batch) return;
+  const int64_t b = t % batch;
+  const TnLeafDesc d = desc[t / batch];
+  real a[3];
+  for (int j = 0; j < 3; ++j) a[j] = d.slot[j] >= 0 ? prm[b * n_params + d.slot[j]] : (real)d.val[j];
+  real m[8];
+  rot_2x2<real>(d.op, a, m);
+  const real sgn = d.conj ? (real)-1 : (real)1;
+  if (d.k == 1) {
+    real* o = leaves + 2 * (d.off * batch + b * 4);
+    for (int i = 0; i < 4; ++i) {
+      o[2 * i] = m[2 * i];
+      o[2 * i + 1] = sgn * m[2 * i + 1];
+    }
+  } else {  // controlled: identity on the control-0 block, m on the control-1 block
+    real* o = leaves + 2 * (d.off * batch + b * 16);
+    for (int r = 0; r < 4; ++r)
+      for (int cidx = 0; cidx < 4; ++cidx) {
+        real re = (r == cidx) ? (real)1 : (real)0, im = 0;
+        if (r >= 2 && cidx >= 2) {
+          re = m[2 * ((r - 2) * 2 + (cidx - 2))];
+          im = m[2 * ((r - 2) * 2 + (cidx - 2)) + 1];
+        }
+        o[2 * (r * 4 + cidx)] = re;
+        o[2 * (r * 4 + cidx) + 1] = sgn * im;
+      }
+  }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ TnGatherArgs A) {
+  const TnGatherOp& o = A.op[blockIdx.y];
+  const int nbits = o.nbits;
+  const int64_t n = 1ll << nbits, total = n * o.nb;
+  const int64_t lmask = (1ll << o.ln) - 1;
+  const int64_t M = 1ll << o.lm, N = 1ll << o.ln, ld = 2 * M;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t >> nbits, e = t & (n - 1);
+    int64_t flat = o.base;
+    for (int j = 0; j < nbits; ++j) flat += ((e >> j) & 1) << o.bit[j];
+    const real* s = static_cast<const real*>(o.src) + b * o.src_bstride;
+    real re, im;
+    if (o.kind == 0) {
+      re = s[2 * flat];
+      im = s[2 * flat + 1];
+    } else {
+      const int64_t i = flat >> o.ln, j = flat & lmask;
+      re = s[j * ld + i] - s[(N + j) * ld + M + i];
+      im = s[(N + j) * ld + i] + s[j * ld + M + i];
+    }
+    real* d = static_cast<real*>(o.dst) + b * 2 * n;
+    d[e] = re;
+    d[n + e] = im;
+  }
+}
+
+template <typename real>
+__global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
+                               real* out, int n_meas, int m, int first, int last) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  const real* p = root + b * bstride;
+  double v = (double)p[0] - (double)p[3];
+  double* a = acc + b * n_meas + m;
+  if (!first) v += *a;
+  *a = v;
+  if (last) out[b * n_meas + m] = (real)v;
+}
+
+}  // namespace
+
+template <typename real>
+cudaError_t tn_build_leaves(const TnLeafDesc* desc, int n_desc, const real* params, int n_params, int64_t batch,
+                            real* leaves, cudaStream_t stream) {
+  const int64_t total = (int64_t)n_desc * batch;
+  if (total == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  return launch_kernel(tn_leaf_kernel<real>, dim3(blocks), dim3(256), 0, stream, desc, n_desc, params, n_params,
+                       batch, leaves);
+}
+
+template <typename real>
+cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
+  int64_t most = 0;
+  for (int i = 0; i < 2; ++i) {
+    const int64_t t = (1ll << args.op[i].nbits) * args.op[i].nb;
+    most = t > most ? t : most;
+  }
+  int64_t blocks = (most + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  return launch_kernel(tn_gather_kernel<real>, dim3((unsigned)blocks, 2), dim3(256), 0, stream, args);
+}
+
+template <typename real>
+cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
+                    int m, int first, int last, cudaStream_t stream) {
+  const unsigned blocks = (unsigned)((batch + 255) / 256);
+  return launch_kernel(tn_root_kernel<real>, dim3(blocks), dim3(256), 0, stream, root, root_bstride, batch, acc, out,
+                       n_meas, m, first, last);
+}
+
+template cudaError_t tn_build_leaves<float>(const TnLeafDesc*, int, const float*, int, int64_t, float*, cudaStream_t);
+template cudaError_t tn_build_leaves<double>(const TnLeafDesc*, int, const double*, int, int64_t, double*,
+                                             cudaStream_t);
+template cudaError_t tn_gather<float>(const TnGatherArgs&, cudaStream_t);
+template cudaError_t tn_gather<double>(const TnGatherArgs&, cudaStream_t);
+template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int, cudaStream_t);
+template cudaError_t tn_root<double>(const double*, int64_t, int64_t, double*, double*, int, int, int, int,
+                                     cudaStream_t);
+
+}  // namespace tedq

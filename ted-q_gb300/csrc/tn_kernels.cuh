@@ -1,0 +1,56 @@
+// tn_kernels.cuh -- device side of the tensor-network mode: batched gate
+// tensors from the parameters, operand gathers (bit permutations into planar
+// real GEMM operands) and the FP64 root accumulation.  The GEMMs themselves
+// are cuBLAS strided-batched calls issued by tn_capi.cpp.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tedq {
+
+// One parameter-dependent gate tensor (ket side, or its conjugate on the bra
+// side), stored for every circuit of the batch at
+// leaves + 2 * (off * batch + b * 4^k) reals.
+struct TnLeafDesc {
+  int32_t op;       // TEDQ_OP_*
+  int32_t k;        // 1 or 2
+  int32_t conj;     // 1: bra side (complex conjugate)
+  int32_t pad;
+  int32_t slot[4];  // parameter slots, -1 = use val
+  double val[4];
+  int64_t off;      // complex elements per batch entry before this tensor
+};
+
+constexpr int kTnMaxBits = 48;
+
+// One GEMM operand: element e of the [F][K] gather (n = F*K entries, nbits =
+// log2 n) takes source flat index base + sum_j bit_j(e) << bit[j]; the real
+// part goes to dst[e], the imaginary part to dst[n + e] (per batch entry).
+struct TnGatherOp {
+  const void* src;
+  void* dst;
+  int64_t src_bstride;  // reals between batch entries of the source (0: shared)
+  int64_t base;         // flat-index offset of the current slice
+  int64_t nb;           // batch entries gathered (1 for a shared operand)
+  int32_t kind;         // 0: interleaved complex leaf, 1: real product (P form)
+  int32_t lm, ln;       // P form: log2 M, log2 N of the producing step
+  int32_t nbits;
+  int8_t bit[kTnMaxBits];
+};
+
+struct TnGatherArgs {
+  TnGatherOp op[2];
+};
+
+template <typename real>
+cudaError_t tn_build_leaves(const TnLeafDesc* desc, int n_desc, const real* params, int n_params, int64_t batch,
+                            real* leaves, cudaStream_t stream);
+template <typename real>
+cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream);
+// acc[b * n_meas + m] (+)= Re(root) for every circuit b (first: assign);
+// last: out[b * n_meas + m] = acc.
+template <typename real>
+cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
+                    int m, int first, int last, cudaStream_t stream);
+
+}  // namespace tedq

@@ -78,6 +78,20 @@ class ServerStats(ctypes.Structure):
                 ("reserved", c_int64 * 4)]
 
 
+class TnOptions(ctypes.Structure):
+    _fields_ = [("precision", c_int32), ("gemm", c_int32), ("max_rank", c_int32), ("repeats", c_int32),
+                ("seed", ctypes.c_uint64), ("graphs", c_int32), ("reserved", c_int32 * 3)]
+
+
+class TnInfo(ctypes.Structure):
+    _fields_ = [("n_qubits", c_int32), ("n_params", c_int32), ("n_meas", c_int32), ("n_steps", c_int32),
+                ("max_rank", c_int32), ("n_sliced", c_int32), ("gates_kept", c_int32), ("precision", c_int32),
+                ("log2_flops", c_double), ("workspace_per_circuit", c_int64), ("workspace_fixed", c_int64),
+                ("reserved", c_int64 * 4)]
+
+
+TN_GEMM = {"bf16x9": 0, "tf32": 1, "fp32": 2}
+
 # every symbol the header declares, with (restype, argtypes)
 SIGNATURES = {
     "tedq_abi_version": (c_int32, []),
@@ -103,6 +117,13 @@ SIGNATURES = {
     "tedq_server_resume": (c_int32, [c_void_p]),
     "tedq_profile_enable": (c_int32, [c_void_p, c_int32]),
     "tedq_profile_read": (c_int32, [c_void_p, POINTER(Profile)]),
+    "tedq_tn_plan_create": (c_int32, [POINTER(Gate), c_int32, c_int32, POINTER(Meas), c_int32, POINTER(TnOptions),
+                                      POINTER(c_void_p)]),
+    "tedq_tn_plan_destroy": (c_int32, [c_void_p]),
+    "tedq_tn_plan_info": (c_int32, [c_void_p, POINTER(TnInfo)]),
+    "tedq_tn_plan_describe": (c_int64, [c_void_p, c_char_p, c_int64]),
+    "tedq_tn_workspace_bytes": (c_int64, [c_void_p, c_int64]),
+    "tedq_tn_contract": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_size_t, c_void_p]),
 }
 
 _lib = None

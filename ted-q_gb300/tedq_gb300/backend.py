@@ -51,11 +51,12 @@ def _cmatrix(m, k):
     return np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1).reshape(-1))
 
 
-class NativeProgram:
-    """Owner of one ``tedq_program_t`` (compile of a recorded circuit)."""
+class _Recorded:
+    """C-ABI arrays (``tedq_gate_t``, ``tedq_meas_t``) of a recorded circuit,
+    with the positional binding of trainable parameters to slots
+    (compiled_circuit.py:492-547)."""
 
-    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0, jit=0):
-        L = _lib.lib()
+    def __init__(self, circuit):
         self.n = int(circuit.num_qubits)
         ops = list(circuit.operators)
         gates = (_lib.Gate * max(1, len(ops)))()
@@ -146,13 +147,25 @@ class NativeProgram:
                 self.layout.append(("state",))
             else:
                 raise NotImplementedError(f"measurement {kind} is not implemented")
+        self.gates, self.n_ops, self.meas, self.n_meas = gates, len(ops), M, len(meas)
+
+
+class NativeProgram:
+    """Owner of one ``tedq_program_t`` (compile of a recorded circuit)."""
+
+    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0, jit=0):
+        L = _lib.lib()
+        rec = _Recorded(circuit)
+        self._rec = rec
+        self.n, self.n_params, self.layout, self.slot_of = rec.n, rec.n_params, rec.layout, rec.slot_of
+        gates, ops_n, M, meas_n = rec.gates, rec.n_ops, rec.meas, rec.n_meas
         opts = _lib.Options()
         opts.precision = _lib.PREC_C128 if precision == "c128" else _lib.PREC_C64
         opts.fuse = 1 if fuse else 0
         opts.tile_qubits = int(tile_qubits)
         opts.jit = int(jit)
         h = ctypes.c_void_p()
-        _lib.check(L.tedq_program_create(gates, len(ops), self.n, M, len(meas), ctypes.byref(opts), ctypes.byref(h)),
+        _lib.check(L.tedq_program_create(gates, ops_n, self.n, M, meas_n, ctypes.byref(opts), ctypes.byref(h)),
                    "tedq_program_create")
         self.handle = h
         info = _lib.ProgramInfo()
@@ -191,6 +204,80 @@ class NativeProgram:
 
     def workspace_bytes(self, batch):
         return int(_lib.lib().tedq_program_workspace_bytes(self.handle, int(batch)))
+
+
+class NativeTnPlan:
+    """Owner of one ``tedq_tn_plan_t``: the tensor-network mode.
+
+    Replaces the TN branch of ``PyTorchBackend.execute`` (pytorch_backend.py
+    :242-356) with its network builder (tensor_network.py:850-1099) and path
+    optimiser (oe_wrapper.py:24-65): one light-cone-reduced sandwich network
+    per expectation value, planned once, contracted for a whole parameter
+    batch per call as gathers + real GEMMs on the tensor cores."""
+
+    def __init__(self, circuit, precision="c64", gemm="bf16x9", max_rank=0, repeats=0, seed=0, graphs=False):
+        L = _lib.lib()
+        if circuit.init_state is not None:
+            raise NotImplementedError("the tensor-network mode starts from |0...0>")
+        rec = _Recorded(circuit)
+        if any(item[0] != "expval" for item in rec.layout):
+            raise NotImplementedError("the tensor-network mode evaluates expectation values only")
+        if gemm not in _lib.TN_GEMM:
+            raise ValueError(f"tn_gemm must be one of {sorted(_lib.TN_GEMM)}")
+        self._rec = rec
+        self.n, self.n_params, self.layout, self.slot_of = rec.n, rec.n_params, rec.layout, rec.slot_of
+        opts = _lib.TnOptions()
+        opts.precision = _lib.PREC_C128 if precision == "c128" else _lib.PREC_C64
+        opts.gemm = _lib.TN_GEMM[gemm]
+        opts.max_rank = int(max_rank)
+        opts.repeats = int(repeats)
+        opts.seed = int(seed)
+        opts.graphs = 1 if graphs else 0
+        h = ctypes.c_void_p()
+        _lib.check(L.tedq_tn_plan_create(rec.gates, rec.n_ops, self.n, rec.meas, rec.n_meas, ctypes.byref(opts),
+                                         ctypes.byref(h)), "tedq_tn_plan_create")
+        self.handle = h
+        info = _lib.TnInfo()
+        _lib.check(L.tedq_tn_plan_info(h, ctypes.byref(info)), "tedq_tn_plan_info")
+        self.info = info
+        if info.n_params != self.n_params:
+            raise RuntimeError(f"native plan has {info.n_params} parameter slots, expected {self.n_params}")
+        self.n_real = info.n_meas
+        self.precision = precision
+        self.rdtype = torch.float64 if precision == "c128" else torch.float32
+        self.cdtype = torch.complex128 if precision == "c128" else torch.complex64
+        self.has_state = False
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.tedq_tn_plan_destroy(h)
+            self.handle = None
+
+    def describe(self):
+        import json
+        L = _lib.lib()
+        need = L.tedq_tn_plan_describe(self.handle, None, 0)
+        buf = ctypes.create_string_buffer(int(need))
+        L.tedq_tn_plan_describe(self.handle, buf, need)
+        return json.loads(buf.value.decode())
+
+    def workspace_bytes(self, batch):
+        return int(_lib.lib().tedq_tn_workspace_bytes(self.handle, int(batch)))
+
+    def run(self, P, ws_cache):
+        """[B, n_params] parameters on a CUDA device -> [B, n_meas] expectation values."""
+        dev = P.device
+        B = P.shape[0]
+        P = P.to(self.rdtype).contiguous()
+        out = torch.empty((B, self.n_real), dtype=self.rdtype, device=dev)
+        ws, wsb = ws_cache.get(self.workspace_bytes(B), dev)
+        L = _lib.lib()
+        with torch.cuda.device(dev):
+            _lib.check(L.tedq_tn_contract(self.handle, ctypes.c_void_p(P.data_ptr() if P.numel() else 0), B,
+                                          ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws or 0), wsb,
+                                          _stream_ptr(dev)), "tedq_tn_contract")
+        return out
 
 
 class _Workspace:
@@ -281,6 +368,27 @@ class GB300ParamShift(torch.autograd.Function):
         return None, grad.to(P.dtype)
 
 
+class GB300TnExecute(torch.autograd.Function):
+    """Tensor-network forward; backward by the parameter-shift rule, all
+    shifted networks of a batch contracted as one batch.  (The reference
+    differentiates its TN mode through torch autograd of the einsum calls;
+    the gradient is the same.)"""
+
+    @staticmethod
+    def forward(ctx, backend, P):
+        out, _ = backend._forward(P)
+        ctx.backend = backend
+        ctx.save_for_backward(P)
+        return out
+
+    @staticmethod
+    def backward(ctx, d_out):
+        (P,) = ctx.saved_tensors
+        jac = ctx.backend.jacobian_param_shift(P.detach())  # [B, n_meas, n_params]
+        grad = torch.einsum("bk,bkp->bp", d_out.to(jac.dtype), jac)
+        return None, grad.to(P.dtype)
+
+
 class GB300Backend:
     """Compiled circuit executed by the GB300 library (see module docstring)."""
 
@@ -321,8 +429,17 @@ class GB300Backend:
             self._trainableparams[op.instance_id] = op.trainable_params
         self._measurements = circuit.measurements
         self._init_state = circuit.init_state
-        self._prog = NativeProgram(circuit, self._precision, fuse=kwargs.get("fuse", True),
-                                   tile_qubits=kwargs.get("tile_qubits", 0), jit=kwargs.get("jit", 0))
+        # tn_mode / use_jdopttn / use_cotengra select the tensor-network path
+        # (pytorch_backend.py:242-356); the native planner replaces the external
+        # path optimisers, so their objects and hyper_opt are not called
+        self._tn = bool(tn_mode or use_jdopttn or use_cotengra)
+        if self._tn:
+            self._prog = NativeTnPlan(circuit, self._precision, gemm=kwargs.get("tn_gemm", "bf16x9"),
+                                      max_rank=kwargs.get("tn_max_rank", 0), repeats=kwargs.get("tn_repeats", 0),
+                                      seed=kwargs.get("tn_seed", 0), graphs=kwargs.get("tn_graphs", False))
+        else:
+            self._prog = NativeProgram(circuit, self._precision, fuse=kwargs.get("fuse", True),
+                                       tile_qubits=kwargs.get("tile_qubits", 0), jit=kwargs.get("jit", 0))
         self._ws = _Workspace()
         self._device = None
         self._init_dev = None
@@ -394,7 +511,7 @@ class GB300Backend:
         return {f: getattr(i, f) for f, _ in i._fields_ if f != "reserved"}
 
     def describe(self, adjoint=False):
-        return self._prog.describe(adjoint)
+        return self._prog.describe() if self._tn else self._prog.describe(adjoint)
 
     @property
     def states_after_measurement(self):
@@ -437,6 +554,8 @@ class GB300Backend:
 
     def _forward(self, P):
         """Native forward on a [B, n_params] parameter tensor on a CUDA device."""
+        if self._tn:
+            return self._prog.run(P, self._ws), None
         prog = self._prog
         dev = P.device
         B = P.shape[0]
@@ -538,6 +657,12 @@ class GB300Backend:
                              f"{tuple(params.shape)}")
         cdev = self._cuda_device(params.device)
         Pc = params.to(cdev)
+        if self._tn:
+            # one expectation value per measurement: the stacked result is [B, M]
+            if not self._requires_grad:
+                with torch.no_grad():
+                    return self._forward(Pc.detach())[0]
+            return GB300TnExecute.apply(self, Pc)
         if not self._requires_grad:
             with torch.no_grad():
                 out, psi = self._forward(Pc.detach())

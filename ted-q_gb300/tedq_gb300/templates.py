@@ -52,3 +52,47 @@ def hea_spec(n_wires, depth, params=None, final_layer=False, measure="z_each"):
             gates.append({"name": "RZ", "qubits": [j], "params": [float(params[2 * depth + 1][j])], "trainable": [0]})
     meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n_wires)]
     return {"n": n_wires, "gates": gates, "meas": meas, "init_state": None}
+
+
+def lattice_bonds(rows, cols, layer):
+    """CZ bonds of one layer of the 2-D lattice circuit: horizontal bonds on
+    even layers and vertical bonds on odd layers, alternating between the two
+    parity classes every second layer, so that each site takes part in at most
+    one CZ per layer."""
+    par = (layer // 2) % 2
+    if layer % 2 == 0:
+        return [(r * cols + c, r * cols + c + 1) for r in range(rows) for c in range(cols - 1) if c % 2 == par]
+    return [(r * cols + c, (r + 1) * cols + c) for r in range(rows - 1) for c in range(cols) if r % 2 == par]
+
+
+def lattice_params(rows, cols, layers, seed=0):
+    """Haar-random SU(2) angles of every site and layer as Rot(phi, theta,
+    omega): phi, omega ~ U[0, 2 pi), cos(theta) ~ U[-1, 1]; shape
+    [layers * rows * cols * 3]."""
+    rng = np.random.default_rng(seed)
+    n = layers * rows * cols
+    phi = rng.uniform(0.0, 2 * np.pi, n)
+    omega = rng.uniform(0.0, 2 * np.pi, n)
+    theta = np.arccos(rng.uniform(-1.0, 1.0, n))
+    return np.stack([phi, theta, omega], axis=1).reshape(-1)
+
+
+def lattice_spec(rows, cols, layers, params=None, seed=0, site=None):
+    """2-D lattice circuit of the tensor-network workload: per layer a
+    trainable Rot on every site, then CZ on the layer's bonds; one output,
+    <Z> on ``site`` (default: the centre site (rows // 2, cols // 2))."""
+    n = rows * cols
+    if params is None:
+        params = lattice_params(rows, cols, layers, seed)
+    params = np.asarray(params, dtype=np.float64).reshape(layers, n, 3)
+    gates = []
+    for l in range(layers):
+        for q in range(n):
+            gates.append({"name": "Rot", "qubits": [q], "params": [float(v) for v in params[l, q]],
+                          "trainable": [0, 1, 2]})
+        for a, b in lattice_bonds(rows, cols, l):
+            gates.append({"name": "CZ", "qubits": [a, b], "params": [], "trainable": []})
+    if site is None:
+        site = (rows // 2) * cols + cols // 2
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [int(site)]}]}]
+    return {"n": n, "gates": gates, "meas": meas, "init_state": None}

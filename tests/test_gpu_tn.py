@@ -1,0 +1,132 @@
+"""GPU parity of the tensor-network mode (cuBLAS GEMMs + gather kernels through
+``tedq_tn_contract``) against the complex128 oracle of the state-vector path
+and the float64 executor of the exported plan.
+
+Tolerances: complex64 with BF16x9 or FP32 GEMMs within 1e-5 (expvals are
+bounded by 1); complex64 with single TF32 products within 5e-3; complex128
+within 1e-12.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import tn_interp
+from test_tn_plan import flat_params, oracle_out, random_spec
+
+pytestmark = pytest.mark.gpu
+
+qai = pytest.importorskip("tedq_gb300")
+from tedq_gb300.templates import hea_spec, lattice_spec  # noqa: E402
+
+DEV = "cuda:0"
+TOL = {("c64", "bf16x9"): 1e-5, ("c64", "fp32"): 1e-5, ("c64", "tf32"): 5e-3, ("c128", "bf16x9"): 1e-12}
+
+
+def _tn(spec, precision="c64", gemm="bf16x9", **kw):
+    return qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, precision=precision,
+                                                      tn_gemm=gemm, **kw)
+
+
+def _rdt(precision):
+    return torch.float64 if precision == "c128" else torch.float32
+
+
+@pytest.fixture(autouse=True)
+def _native_loaded():
+    yield
+    assert qai._lib._lib is not None, "native library was not used"
+
+
+@pytest.mark.parametrize("mode", [("c64", "bf16x9"), ("c64", "fp32"), ("c64", "tf32"), ("c128", "bf16x9")],
+                         ids=["c64-bf16x9", "c64-fp32", "c64-tf32", "c128"])
+@pytest.mark.parametrize("seed", range(6))
+def test_tn_random_circuits(seed, mode):
+    precision, gemm = mode
+    spec = random_spec(seed)
+    cc = _tn(spec, precision, gemm, requires_grad=False)
+    prm = flat_params(spec)
+    rng = np.random.default_rng(seed)
+    rows = [prm] + [list(rng.uniform(0, 2 * np.pi, len(prm))) for _ in range(4)]
+    P = torch.tensor(rows, dtype=_rdt(precision), device=DEV).reshape(len(rows), len(prm))
+    got = cc.execute_batch(P).cpu().numpy()
+    want = np.stack([oracle_out(spec, r) for r in rows])
+    tol = TOL[mode]
+    np.testing.assert_allclose(got, want, atol=tol, rtol=tol)
+
+
+def test_tn_matches_state_vector_hea():
+    spec = hea_spec(10, 4)
+    spec["meas"] = spec["meas"][:3] + [{"kind": "expval", "list": True,
+                                        "obs": [{"name": "PauliZ", "qubits": [0]}, {"name": "PauliX", "qubits": [9]}]}]
+    prm = np.random.default_rng(7).uniform(0, 2 * np.pi, (16, len(flat_params(spec))))
+    P = torch.tensor(prm, dtype=torch.float32, device=DEV)
+    sv = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)
+    tn = _tn(spec, requires_grad=False)
+    np.testing.assert_allclose(tn.execute_batch(P).cpu().numpy(), sv.execute_batch(P).cpu().numpy(),
+                               atol=1e-5, rtol=1e-5)
+
+
+def test_tn_slicing_on_device():
+    spec = random_spec(53, n=6, n_gates=40)
+    prm = flat_params(spec)
+    cc = _tn(spec, "c128", requires_grad=False)
+    target = cc.program_info["max_rank"] - 1
+    sl = _tn(spec, "c128", tn_max_rank=target, requires_grad=False)
+    assert sl.program_info["n_sliced"] >= 1
+    P = torch.tensor([prm], dtype=torch.float64, device=DEV)
+    np.testing.assert_allclose(sl.execute_batch(P).cpu().numpy()[0], oracle_out(spec, prm), atol=1e-12, rtol=1e-12)
+
+
+def test_tn_lattice_6x6_centre_z():
+    """The 6x6, 8-layer workload: complex64 (BF16x9 GEMMs) against complex128 on
+    the device, and complex128 against the float64 plan executor."""
+    spec = lattice_spec(6, 6, 8, seed=0)
+    prm = flat_params(spec)
+    rng = np.random.default_rng(1)
+    rows = np.stack([prm] + [rng.uniform(0, 2 * np.pi, len(prm)) for _ in range(3)])
+    c128 = _tn(spec, "c128", requires_grad=False)
+    v128 = c128.execute_batch(torch.tensor(rows, dtype=torch.float64, device=DEV)).cpu().numpy()[:, 0]
+    want = tn_interp.run(c128.describe(), prm)[0]
+    assert abs(v128[0] - want) < 1e-12
+    c64 = _tn(spec, "c64", requires_grad=False)
+    v64 = c64.execute_batch(torch.tensor(rows, dtype=torch.float32, device=DEV)).cpu().numpy()[:, 0]
+    np.testing.assert_allclose(v64, v128, atol=1e-5, rtol=1e-5)
+
+
+def test_tn_graph_replay_follows_parameters():
+    spec = lattice_spec(3, 3, 4, seed=2)
+    prm = np.asarray(flat_params(spec))
+    cc = _tn(spec, "c64", tn_graphs=True, requires_grad=False)
+    P = torch.tensor(np.stack([prm, prm * 0.5]), dtype=torch.float32, device=DEV)
+    outs = []
+    for k in range(4):  # eager, capture, replay, replay with new values in the same buffer
+        if k == 3:
+            P.mul_(0.25)
+        outs.append(cc.execute_batch(P).cpu().numpy())
+    np.testing.assert_allclose(outs[1], outs[0], atol=0, rtol=0)
+    np.testing.assert_allclose(outs[2], outs[0], atol=0, rtol=0)
+    want = np.stack([oracle_out(spec, r) for r in P.double().cpu().numpy()])
+    np.testing.assert_allclose(outs[3], want, atol=1e-5, rtol=1e-5)
+
+
+def test_tn_gradient_matches_adjoint():
+    spec = random_spec(4)
+    prm = flat_params(spec)
+    sv = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", precision="c128")
+    tn = _tn(spec, "c128")
+    p1 = torch.tensor(prm, dtype=torch.float64, device=DEV, requires_grad=True)
+    p2 = torch.tensor(prm, dtype=torch.float64, device=DEV, requires_grad=True)
+    sv(p1).sum().backward()
+    tn(p2).sum().backward()
+    np.testing.assert_allclose(p2.grad.cpu().numpy(), p1.grad.cpu().numpy(), atol=1e-10, rtol=1e-10)
+
+
+def test_tn_workspace_and_errors():
+    spec = random_spec(2)
+    cc = _tn(spec, requires_grad=False)
+    prog = cc._prog
+    assert prog.workspace_bytes(4) > prog.workspace_bytes(1)
+    P = torch.zeros((1, prog.n_params + 1), device=DEV)
+    with pytest.raises(ValueError):
+        cc.execute_batch(P)
