@@ -18,6 +18,7 @@ autograd, restated in ``oracle/``) on the host CPU cores.
 """
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -467,6 +468,164 @@ def run_serving(a):
     return 0
 
 
+# ---------------------------------------------------------------- tensor-network workload
+
+TN_METRIC = "6x6 lattice 8-layer centre <Z> tensor-network contractions/s"
+
+
+def tn_params(rows, cols, layers, count, seed):
+    """Haar-random Rot angles, [count, layers * rows * cols * 3]."""
+    from tedq_gb300.templates import lattice_params
+    return np.stack([lattice_params(rows, cols, layers, seed * 100003 + i) for i in range(count)])
+
+
+def tn_cpu_rate(spec, prm_rows, dtype):
+    """Reference TN algorithm on the host (sandwich network, greedy pairwise
+    order, tensordot contractions; oracle/tn_oracle.py).  The order is computed
+    once outside the timed loop, as the reference's contract_expression does."""
+    from oracle import tn_oracle
+    arrays, idx = tn_oracle.network(spec, list(prm_rows[0]))
+    order = tn_oracle.greedy_order(idx)
+    t0 = time.perf_counter()
+    vals = []
+    for row in prm_rows:
+        arrays, idx = tn_oracle.network(spec, list(row))
+        vals.append(tn_oracle.contract(arrays, idx, order, dtype).real)
+    dt = time.perf_counter() - t0
+    return len(prm_rows) / dt, dt, np.array(vals)
+
+
+def run_tn(a):
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    import tedq_gb300 as qai
+    from tedq_gb300 import _lib
+    from tedq_gb300.templates import lattice_spec
+
+    R, C, Lr = 6, 6, 8
+    spec = lattice_spec(R, C, Lr, seed=0)
+    B = a.batch
+    t_plan = time.perf_counter()
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, tn_gemm=a.tn_gemm,
+                                                    tn_graphs=True, requires_grad=False)
+    t_plan = time.perf_counter() - t_plan
+    info = cc.program_info
+    P = info["n_params"]
+    params_host = torch.tensor(tn_params(R, C, Lr, (a.steps + a.warmup) * B, 1000 + rank),
+                               dtype=torch.float32).reshape(a.steps + a.warmup, B, P)
+    params_dev = params_host.to(dev)
+    outs = [torch.empty((B, 1), dtype=torch.float32, device=dev) for _ in range(a.steps + a.warmup)]
+    L = _lib.lib()
+    prog = cc._prog
+    stream = torch.cuda.current_stream(dev)
+    ws, wsb = cc._ws.get(prog.workspace_bytes(B), dev)
+
+    def step(i):  # the public C entry point on device-resident buffers (graph replay after the 2nd call)
+        _lib.check(L.tedq_tn_contract(prog.handle, ctypes.c_void_p(params_dev[i].data_ptr()), B,
+                                      ctypes.c_void_p(outs[i].data_ptr()), ctypes.c_void_p(ws), wsb,
+                                      ctypes.c_void_p(stream.cuda_stream)), "tedq_tn_contract")
+
+    # every timed step uses its own parameter and output buffers: capture each
+    # graph during warm-up (two calls per buffer set: eager, then captured)
+    for i in range(a.warmup + a.steps):
+        step(i)
+        step(i)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(a.steps):
+        step(a.warmup + i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
+    value = world * B * a.steps / (ms / 1000.0)
+
+    # kernel timing: events around every launch (eager, same workload)
+    L.tedq_tn_profile_enable(prog.handle, 1)
+    for i in range(a.steps):
+        step(a.warmup + i)
+    torch.cuda.synchronize()
+    L.tedq_tn_profile_enable(prog.handle, 0)
+    prof = _lib.TnProfile()
+    _lib.check(L.tedq_tn_profile_read(prog.handle, ctypes.byref(prof)), "tedq_tn_profile_read")
+
+    # e2e through the public API: pinned host parameters in, host results out
+    ph = params_host.pin_memory()
+    for i in range(min(2, a.warmup)):
+        cc.execute_batch(ph[i]).cpu()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        res = cc.execute_batch(ph[a.warmup + i]).cpu()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms_e2e = max_over_ranks(1000 * wall, world, dev)
+    e2e = world * B * a.steps / (ms_e2e / 1000.0)
+
+    if rank != 0:
+        return 0
+    # accuracy: complex64 (this GEMM mode) against complex128 on the device and the CPU oracle
+    ref = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, precision="c128",
+                                                      requires_grad=False)
+    v128 = ref.execute_batch(params_dev[0].double()).cpu().numpy()[:, 0]
+    v64 = outs[0].cpu().numpy()[:, 0]
+    peak_kind = "measured"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        bf16, peak_kind = 1900.0, "fallback"
+    if a.tn_gemm == "bf16x9":
+        peak = bf16 / 9.0
+        peak_kind += " bf16 dense / 9 (each FP32 product is 9 BF16 tensor-core products)"
+    elif a.tn_gemm == "tf32":
+        peak = bf16 / 2.0
+        peak_kind += " bf16 dense / 2 (TF32 rate)"
+    else:
+        peak = None
+        peak_kind = "FP32 SIMT (no tensor-core peak)"
+    achieved = prof.gemm_flops / (prof.gemm_ms / 1000.0) / 1e12 if prof.gemm_ms else 0.0
+    per_call = prof.leaf_launches + prof.gather_launches + prof.gemm_launches + prof.root_launches
+    line = {"metric": TN_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": f"c64 ({a.tn_gemm} GEMM, FP32 accumulate)", "data": "synthetic",
+            "config": {"workload": f"tn_lattice{R}x{C}_{Lr}layers_centreZ_batch{B}", "sites": R * C, "layers": Lr,
+                       "gates": len(spec["gates"]), "gates_in_light_cone": info["gates_kept"],
+                       "params_per_circuit": P, "contractions_per_circuit": info["n_steps"],
+                       "largest_intermediate_log2": info["max_rank"], "sliced": info["n_sliced"],
+                       "flops_per_circuit": 2.0 ** info["log2_flops"], "batch_per_gpu": B,
+                       "plan_s": round(t_plan, 3), "graphs": True,
+                       "l2": "inputs larger than L2 (intermediates %.1f GB per step)" %
+                             (prog.workspace_bytes(B) / 1e9)},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4, "d2h_bytes_per_step": B * 4},
+            "gpu_launches": int(per_call),
+            "roofline": {"bound": "tensor", "kernel": "cuBLAS strided-batched GEMM (4M real decomposition)",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if peak else None, "traffic": None, "peak_kind": peak_kind,
+                         "gemm_ms_per_step": prof.gemm_ms / a.steps, "gather_ms_per_step": prof.gather_ms / a.steps,
+                         "gather_gbs": prof.gather_bytes / (prof.gather_ms / 1000.0) / 1e9 if prof.gather_ms else 0,
+                         "leaf_ms_per_step": prof.leaf_ms / a.steps, "root_ms_per_step": prof.root_ms / a.steps,
+                         "launches_per_step": per_call / a.steps},
+            "accuracy": {"max_abs_err_vs_c128": float(np.abs(v64 - v128).max())},
+            "clocks": clk}
+    if not a.no_cpu:
+        rows = params_host[0, : max(1, a.tn_cpu_circuits)].double().numpy()
+        rate, dt, vcpu = tn_cpu_rate(spec, rows, np.complex64)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": f"{len(rows)} circuit(s), complex64 tensordot contractions, {dt:.1f} s"}
+        _, _, v128cpu = tn_cpu_rate(spec, rows[:2], np.complex128)
+        line["accuracy"]["max_abs_err_vs_cpu_c128"] = float(np.abs(v64[:2] - v128cpu).max())
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -479,7 +638,9 @@ def main():
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
-    ap.add_argument("--workload", default="vqc", choices=["vqc", "serving"])
+    ap.add_argument("--workload", default="vqc", choices=["vqc", "serving", "tn"])
+    ap.add_argument("--tn-gemm", default="bf16x9", choices=["bf16x9", "tf32", "fp32"])
+    ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--rates", default="100,500,2000,5000")
     ap.add_argument("--duration", type=float, default=2.0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
@@ -491,6 +652,8 @@ def main():
         return run_reference_arm(a)
     if a.workload == "serving":
         return run_serving(a)
+    if a.workload == "tn":
+        return run_tn(a)
     return run_ours(a)
 
 

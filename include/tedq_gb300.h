@@ -343,6 +343,28 @@ int64_t tedq_tn_workspace_bytes(const tedq_tn_plan_t* plan, int64_t batch);
 int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch, void* out,
                          void* workspace, size_t workspace_bytes, void* stream);
 
+/* Kernel timing of tedq_tn_contract (no counterpart in the reference): while
+ * enabled, calls run without graphs and record CUDA events around every launch
+ * on the launch stream; read sums the durations per launch family since the
+ * last read, with the algorithmic work of the launches (gather bytes: source
+ * read + planar operand write; GEMM flops: 2 per real multiply-add). */
+typedef struct tedq_tn_profile {
+  int64_t leaf_launches;
+  double leaf_ms;
+  int64_t gather_launches;
+  double gather_ms;
+  double gather_bytes;
+  int64_t gemm_launches;
+  double gemm_ms;
+  double gemm_flops;
+  int64_t root_launches;
+  double root_ms;
+  int64_t reserved[4];
+} tedq_tn_profile_t;
+
+int32_t tedq_tn_profile_enable(tedq_tn_plan_t* plan, int32_t on);
+int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,15 @@ struct tedq_tn_plan {
   int64_t const_total = 0, desc_total = 0;
   std::mutex mu;
   TnDevice dev[64];
+  // kernel timing (tedq_tn_profile_*)
+  struct Ev {
+    cudaEvent_t a, b;
+    int family;  // 0 leaf, 1 gather, 2 gemm, 3 root
+    double work;
+  };
+  bool profiling = false;
+  std::vector<Ev> events;
+  std::mutex prof_mu;
 };
 
 namespace {
@@ -211,6 +220,21 @@ int32_t ensure_device(tedq_tn_plan* p, int dev) {
   return TEDQ_OK;
 }
 
+// Runs one launch; with profiling on, brackets it with events on its stream.
+template <typename F>
+int32_t timed(tedq_tn_plan* p, cudaStream_t s, int family, double work, F&& launch) {
+  if (!p->profiling) return launch();
+  tedq_tn_plan::Ev ev{nullptr, nullptr, family, work};
+  TEDQ_CUDA("tedq_tn_contract: cudaEventCreate", cudaEventCreate(&ev.a));
+  TEDQ_CUDA("tedq_tn_contract: cudaEventCreate", cudaEventCreate(&ev.b));
+  TEDQ_CUDA("tedq_tn_contract: cudaEventRecord", cudaEventRecord(ev.a, s));
+  int32_t rc = launch();
+  TEDQ_CUDA("tedq_tn_contract: cudaEventRecord", cudaEventRecord(ev.b, s));
+  std::lock_guard<std::mutex> lk(p->prof_mu);
+  p->events.push_back(ev);
+  return rc;
+}
+
 // Enqueues one call: batched gate tensors, then per network and slice the
 // gathers and GEMMs of every step and the FP64 root accumulation.
 template <typename real>
@@ -239,10 +263,15 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
   for (int m = 0; m < n_meas; ++m) {
     const TnNet& net = p->nets[m];
     const real* consts = static_cast<const real*>(D.consts) + p->const_base[m];
-    if (!p->descs[m].empty())
-      TEDQ_CUDA("tedq_tn_contract: leaf kernel",
-                tn_build_leaves<real>(D.desc + p->desc_base[m], (int)p->descs[m].size(), params, p->n_params,
-                                      batch, leaves, s));
+    if (!p->descs[m].empty()) {
+      int32_t rc = timed(p, s, 0, 0.0, [&]() -> int32_t {
+        TEDQ_CUDA("tedq_tn_contract: leaf kernel",
+                  tn_build_leaves<real>(D.desc + p->desc_base[m], (int)p->descs[m].size(), params, p->n_params,
+                                        batch, leaves, s));
+        return TEDQ_OK;
+      });
+      if (rc != TEDQ_OK) return rc;
+    }
     auto source = [&](int t, TnGatherOp& o) {
       const TnTensor& T = net.tensors[t];
       if (T.leaf >= 0) {
@@ -277,19 +306,38 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         }
         A.op[0].dst = scratch;
         A.op[1].dst = scratch + (2ll << A.op[0].nbits) * A.op[0].nb;
-        TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_gather<real>(A, s));
+        double gbytes = 0;
+        for (int x = 0; x < 2; ++x) {
+          const TnGatherOp& o = A.op[x];
+          gbytes += (double)o.nb * (double)(1ll << o.nbits) * sizeof(real) * (o.kind == 0 ? 4.0 : 6.0);
+        }
+        int32_t rc = timed(p, s, 1, gbytes, [&]() -> int32_t {
+          TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_gather<real>(A, s));
+          return TEDQ_OK;
+        });
+        if (rc != TEDQ_OK) return rc;
         const TnTensor& T = net.tensors[stp.out];
         const long long M = 1ll << stp.opa.nf, N = 1ll << stp.opb.nf, K = 1ll << stp.opa.nc;
         real* C = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
-        st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)(2 * M), (int)(2 * N), (int)K, &one, A.op[0].dst, dt,
-                     (int)K, A.op[0].nb > 1 ? 2 * M * K : 0, A.op[1].dst, dt, (int)K, A.op[1].nb > 1 ? 2 * N * K : 0,
-                     &zero, C, dt, (int)(2 * M), 4 * M * N, stp.batched ? (int)batch : 1, ct, CUBLAS_GEMM_DEFAULT);
-        if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
+        const int nbatch = stp.batched ? (int)batch : 1;
+        rc = timed(p, s, 2, 8.0 * M * N * K * nbatch, [&]() -> int32_t {
+          st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)(2 * M), (int)(2 * N), (int)K, &one, A.op[0].dst, dt,
+                       (int)K, A.op[0].nb > 1 ? 2 * M * K : 0, A.op[1].dst, dt, (int)K,
+                       A.op[1].nb > 1 ? 2 * N * K : 0, &zero, C, dt, (int)(2 * M), 4 * M * N, nbatch, ct,
+                       CUBLAS_GEMM_DEFAULT);
+          if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
+          return TEDQ_OK;
+        });
+        if (rc != TEDQ_OK) return rc;
       }
       const TnTensor& R = net.tensors[net.root];
       const real* root = R.batched ? arena_b + R.arena * batch : arena_u + R.arena;
-      TEDQ_CUDA("tedq_tn_contract: root kernel",
-                tn_root<real>(root, R.batched ? 4 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
+      int32_t rc = timed(p, s, 3, 0.0, [&]() -> int32_t {
+        TEDQ_CUDA("tedq_tn_contract: root kernel",
+                  tn_root<real>(root, R.batched ? 4 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
+        return TEDQ_OK;
+      });
+      if (rc != TEDQ_OK) return rc;
     }
   }
   return TEDQ_OK;
@@ -300,7 +348,7 @@ int32_t contract(tedq_tn_plan* p, TnDevice& D, const void* params, int64_t batch
                  cudaStream_t s) {
   const real* prm = static_cast<const real*>(params);
   real* o = static_cast<real*>(out);
-  if (!p->graphs) return enqueue<real>(p, D, prm, batch, o, ws, s);
+  if (!p->graphs || p->profiling) return enqueue<real>(p, D, prm, batch, o, ws, s);
   const bool same = D.g_params == params && D.g_out == out && D.g_ws == ws && D.g_batch == batch;
   if (!same) {
     // new arguments: run eagerly, capture on the next call with the same ones
@@ -505,6 +553,39 @@ int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch
   } catch (const std::exception& e) {
     return fail(TEDQ_ERR_ARG, std::string("tedq_tn_contract: ") + e.what());
   }
+}
+
+int32_t tedq_tn_profile_enable(tedq_tn_plan_t* plan, int32_t on) {
+  if (!plan) return fail(TEDQ_ERR_ARG, "tedq_tn_profile_enable: plan is null");
+  std::lock_guard<std::mutex> lk(plan->mu);
+  plan->profiling = on != 0;
+  return TEDQ_OK;
+}
+
+int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out) {
+  if (!plan || !out) return fail(TEDQ_ERR_ARG, "tedq_tn_profile_read: null argument");
+  std::vector<tedq_tn_plan::Ev> evs;
+  {
+    std::lock_guard<std::mutex> lk(plan->prof_mu);
+    evs.swap(plan->events);
+  }
+  std::memset(out, 0, sizeof(*out));
+  int32_t rc = TEDQ_OK;
+  for (auto& e : evs) {
+    float ms = 0;
+    cudaError_t err = cudaEventSynchronize(e.b);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e.a, e.b);
+    if (err != cudaSuccess && rc == TEDQ_OK) rc = cuda_fail("tedq_tn_profile_read", err);
+    switch (e.family) {
+      case 0: out->leaf_launches++; out->leaf_ms += ms; break;
+      case 1: out->gather_launches++; out->gather_ms += ms; out->gather_bytes += e.work; break;
+      case 2: out->gemm_launches++; out->gemm_ms += ms; out->gemm_flops += e.work; break;
+      default: out->root_launches++; out->root_ms += ms; break;
+    }
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  return rc;
 }
 
 }  // extern "C"

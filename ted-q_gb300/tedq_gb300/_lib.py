@@ -90,6 +90,13 @@ class TnInfo(ctypes.Structure):
                 ("reserved", c_int64 * 4)]
 
 
+class TnProfile(ctypes.Structure):
+    _fields_ = [("leaf_launches", c_int64), ("leaf_ms", c_double), ("gather_launches", c_int64),
+                ("gather_ms", c_double), ("gather_bytes", c_double), ("gemm_launches", c_int64),
+                ("gemm_ms", c_double), ("gemm_flops", c_double), ("root_launches", c_int64), ("root_ms", c_double),
+                ("reserved", c_int64 * 4)]
+
+
 TN_GEMM = {"bf16x9": 0, "tf32": 1, "fp32": 2}
 
 # every symbol the header declares, with (restype, argtypes)
@@ -124,6 +131,8 @@ SIGNATURES = {
     "tedq_tn_plan_describe": (c_int64, [c_void_p, c_char_p, c_int64]),
     "tedq_tn_workspace_bytes": (c_int64, [c_void_p, c_int64]),
     "tedq_tn_contract": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tedq_tn_profile_enable": (c_int32, [c_void_p, c_int32]),
+    "tedq_tn_profile_read": (c_int32, [c_void_p, POINTER(TnProfile)]),
 }
 
 _lib = None

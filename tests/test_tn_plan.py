@@ -198,3 +198,15 @@ def test_tn_mode_rejects_non_expval():
     spec["meas"] = [{"kind": "probs", "qubits": [0]}]
     with pytest.raises(NotImplementedError):
         plan(spec)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_tn_oracle_matches_state_vector_oracle(seed):
+    """The CPU tensor-network restatement (full and light-cone networks) agrees
+    with the state-vector oracle."""
+    from oracle import tn_oracle
+    spec = random_spec(seed + 20)
+    prm = flat_params(spec)
+    want = oracle_out(spec, prm)
+    np.testing.assert_allclose(tn_oracle.expval(spec, prm), want, atol=1e-12, rtol=1e-12)
+    np.testing.assert_allclose(tn_oracle.expval(spec, prm, light_cone=False), want, atol=1e-12, rtol=1e-12)
