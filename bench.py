@@ -582,7 +582,7 @@ def run_tn(a):
             bf16 = float(json.load(f)["bf16_tflops"])
     except Exception:
         bf16, peak_kind = 1900.0, "fallback"
-    if a.tn_gemm == "bf16x9":
+    if a.tn_gemm in ("bf16x9", "auto"):
         peak = bf16 / 9.0
         peak_kind += " bf16 dense / 9 (each FP32 product is 9 BF16 tensor-core products)"
     elif a.tn_gemm == "tf32":
@@ -639,7 +639,7 @@ def main():
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
     ap.add_argument("--workload", default="vqc", choices=["vqc", "serving", "tn"])
-    ap.add_argument("--tn-gemm", default="bf16x9", choices=["bf16x9", "tf32", "fp32"])
+    ap.add_argument("--tn-gemm", default="bf16x9", choices=["bf16x9", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--rates", default="100,500,2000,5000")
     ap.add_argument("--duration", type=float, default=2.0)

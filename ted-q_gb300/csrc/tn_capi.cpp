@@ -190,8 +190,9 @@ int32_t ensure_device(tedq_tn_plan* p, int dev) {
   if (!D.handle) {
     cublasStatus_t st = B.create(&D.handle);
     if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasCreate", st);
-    if (p->precision == TEDQ_PREC_C64 && p->gemm == TEDQ_TN_GEMM_BF16X9) {
-      st = B.set_emulation(D.handle, CUBLAS_EMULATION_STRATEGY_EAGER);
+    if (p->precision == TEDQ_PREC_C64 && (p->gemm == TEDQ_TN_GEMM_BF16X9 || p->gemm == TEDQ_TN_GEMM_AUTO)) {
+      st = B.set_emulation(D.handle, p->gemm == TEDQ_TN_GEMM_AUTO ? CUBLAS_EMULATION_STRATEGY_PERFORMANT
+                                                                  : CUBLAS_EMULATION_STRATEGY_EAGER);
       if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetEmulationStrategy", st);
     }
   }
@@ -276,15 +277,17 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       const TnTensor& T = net.tensors[t];
       if (T.leaf >= 0) {
         o.kind = 0;
-        o.lm = o.ln = 0;
+        o.lm = 0;
         o.src = T.batched ? leaves + 2 * T.off * batch : consts + 2 * T.off;
         o.src_bstride = T.batched ? (2ll << T.full_idx.size()) : 0;
       } else {
         o.kind = 1;
         o.lm = T.lm;
-        o.ln = T.ln;
+        const int64_t M = 1ll << T.lm, N = 1ll << T.ln;
+        o.sj = T.split ? 2 * M : M;
+        o.sp = T.split ? M : M * N;
         o.src = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
-        o.src_bstride = T.batched ? (4ll << (T.lm + T.ln)) : 0;
+        o.src_bstride = T.batched ? (2ll << (T.lm + T.ln)) : 0;
       }
     };
     const int64_t n_slices = 1ll << net.sliced.size();
@@ -303,13 +306,15 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
           o.base = 0;
           for (auto& qb : op.slice_bit) o.base += ((sl >> qb.first) & 1) << qb.second;
           o.nb = net.tensors[op.tensor].batched ? batch : 1;
+          o.nc = op.nc;
+          o.doubled = op.doubled ? 1 : 0;
         }
         A.op[0].dst = scratch;
-        A.op[1].dst = scratch + (2ll << A.op[0].nbits) * A.op[0].nb;
+        A.op[1].dst = scratch + ((A.op[0].doubled ? 4ll : 2ll) << A.op[0].nbits) * A.op[0].nb;
         double gbytes = 0;
         for (int x = 0; x < 2; ++x) {
           const TnGatherOp& o = A.op[x];
-          gbytes += (double)o.nb * (double)(1ll << o.nbits) * sizeof(real) * (o.kind == 0 ? 4.0 : 6.0);
+          gbytes += (double)o.nb * (double)(1ll << o.nbits) * sizeof(real) * (o.doubled ? 6.0 : 4.0);
         }
         int32_t rc = timed(p, s, 1, gbytes, [&]() -> int32_t {
           TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_gather<real>(A, s));
@@ -320,11 +325,14 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         const long long M = 1ll << stp.opa.nf, N = 1ll << stp.opb.nf, K = 1ll << stp.opa.nc;
         real* C = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
         const int nbatch = stp.batched ? (int)batch : 1;
+        // real embedding: [Re A, Im A] x [[Re B, Im B], [-Im B, Re B]] (B doubled) or
+        // [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B] (A doubled); K is doubled either way
+        const long long mr = stp.double_a ? 2 * M : M, nr = stp.double_a ? N : 2 * N;
+        const long long sa = A.op[0].nb > 1 ? mr * 2 * K : 0, sb = A.op[1].nb > 1 ? nr * 2 * K : 0;
         rc = timed(p, s, 2, 8.0 * M * N * K * nbatch, [&]() -> int32_t {
-          st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)(2 * M), (int)(2 * N), (int)K, &one, A.op[0].dst, dt,
-                       (int)K, A.op[0].nb > 1 ? 2 * M * K : 0, A.op[1].dst, dt, (int)K,
-                       A.op[1].nb > 1 ? 2 * N * K : 0, &zero, C, dt, (int)(2 * M), 4 * M * N, nbatch, ct,
-                       CUBLAS_GEMM_DEFAULT);
+          st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)mr, (int)nr, (int)(2 * K), &one, A.op[0].dst, dt,
+                       (int)(2 * K), sa, A.op[1].dst, dt, (int)(2 * K), sb, &zero, C, dt, (int)mr, 2 * M * N, nbatch,
+                       ct, CUBLAS_GEMM_DEFAULT);
           if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
           return TEDQ_OK;
         });
@@ -334,7 +342,7 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       const real* root = R.batched ? arena_b + R.arena * batch : arena_u + R.arena;
       int32_t rc = timed(p, s, 3, 0.0, [&]() -> int32_t {
         TEDQ_CUDA("tedq_tn_contract: root kernel",
-                  tn_root<real>(root, R.batched ? 4 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
+                  tn_root<real>(root, R.batched ? 2 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
         return TEDQ_OK;
       });
       if (rc != TEDQ_OK) return rc;
@@ -415,7 +423,7 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
     if (opts) {
       if (opts->precision != TEDQ_PREC_C64 && opts->precision != TEDQ_PREC_C128)
         throw std::invalid_argument("unknown precision");
-      if (opts->gemm < TEDQ_TN_GEMM_BF16X9 || opts->gemm > TEDQ_TN_GEMM_FP32)
+      if (opts->gemm < TEDQ_TN_GEMM_BF16X9 || opts->gemm > TEDQ_TN_GEMM_AUTO)
         throw std::invalid_argument("unknown GEMM mode");
       if (opts->max_rank < 0 || opts->max_rank > 34) throw std::invalid_argument("max_rank out of range");
       p->precision = opts->precision;

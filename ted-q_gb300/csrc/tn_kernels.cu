@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   const TnGatherOp& o = A.op[blockIdx.y];
   const int nbits = o.nbits;
   const int64_t n = 1ll << nbits, total = n * o.nb;
-  const int64_t lmask = (1ll << o.ln) - 1;
-  const int64_t M = 1ll << o.lm, N = 1ll << o.ln, ld = 2 * M;
+  const int64_t K = 1ll << o.nc, imask = (1ll << o.lm) - 1;
+  const int64_t dstride = (o.doubled ? 4 : 2) * n;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = t >> nbits, e = t & (n - 1);
     int64_t flat = o.base;
@@ -113,13 +113,21 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
       re = s[2 * flat];
       im = s[2 * flat + 1];
     } else {
-      const int64_t i = flat >> o.ln, j = flat & lmask;
-      re = s[j * ld + i] - s[(N + j) * ld + M + i];
-      im = s[(N + j) * ld + i] + s[j * ld + M + i];
+      const int64_t at = (flat >> o.lm) * o.sj + (flat & imask);
+      re = s[at];
+      im = s[at + o.sp];
     }
-    real* d = static_cast<real*>(o.dst) + b * 2 * n;
-    d[e] = re;
-    d[n + e] = im;
+    real* d = static_cast<real*>(o.dst) + b * dstride;
+    const int64_t f = e >> o.nc, k = e & (K - 1);
+    real* row = d + f * 2 * K + k;
+    row[0] = re;
+    if (!o.doubled) {
+      row[K] = im;
+    } else {
+      row[K] = -im;
+      row[n * 2] = im;  // row F + f
+      row[n * 2 + K] = re;
+    }
   }
 }
 
@@ -129,7 +137,7 @@ __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, i
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= batch) return;
   const real* p = root + b * bstride;
-  double v = (double)p[0] - (double)p[3];
+  double v = (double)p[0];
   double* a = acc + b * n_meas + m;
   if (!first) v += *a;
   *a = v;

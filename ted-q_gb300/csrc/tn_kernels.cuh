@@ -23,18 +23,22 @@ struct TnLeafDesc {
 
 constexpr int kTnMaxBits = 48;
 
-// One GEMM operand: element e of the [F][K] gather (n = F*K entries, nbits =
-// log2 n) takes source flat index base + sum_j bit_j(e) << bit[j]; the real
-// part goes to dst[e], the imaginary part to dst[n + e] (per batch entry).
+// One GEMM operand: element e = f*K + k of the gather (n = F*K entries, nbits =
+// log2 n, K = 2^nc) takes source flat index base + sum_j bit_j(e) << bit[j].
+// Output rows of 2K reals: row f = [Re(f, 0..K), Im(f, 0..K)]; a doubled
+// operand writes [Re, -Im] in row f and [Im, Re] in row F + f.
 struct TnGatherOp {
   const void* src;
   void* dst;
   int64_t src_bstride;  // reals between batch entries of the source (0: shared)
   int64_t base;         // flat-index offset of the current slice
   int64_t nb;           // batch entries gathered (1 for a shared operand)
-  int32_t kind;         // 0: interleaved complex leaf, 1: real product (P form)
-  int32_t lm, ln;       // P form: log2 M, log2 N of the producing step
-  int32_t nbits;
+  int64_t sj, sp;       // intermediate source: Re(i, j) at j*sj + i, Im at + sp
+  int32_t kind;         // 0: interleaved complex leaf, 1: intermediate
+  int32_t lm;           // intermediate source: log2 of its i extent
+  int32_t nbits, nc;
+  int32_t doubled;
+  int32_t pad;
   int8_t bit[kTnMaxBits];
 };
 

@@ -424,7 +424,7 @@ struct Arena {
   }
 };
 
-static int64_t inter_reals(const TnTensor& t) { return 4ll << (t.lm + t.ln); }
+static int64_t inter_reals(const TnTensor& t) { return 2ll << (t.lm + t.ln); }
 
 TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_meas_t& meas,
                const TnPlanOptions& opt) {
@@ -525,9 +525,17 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
     for (int i : B)
       if (std::find(A.begin(), A.end(), i) == A.end()) st.free_b.push_back(i);
     st.batched = net.tensors[st.a].batched || net.tensors[st.b].batched;
+    // the doubled operand is the one with fewer stored entries (batched
+    // operands count as many circuits)
+    {
+      const double wa = std::ldexp(net.tensors[st.a].batched ? 1048576.0 : 1.0, (int)st.free_a.size());
+      const double wb = std::ldexp(net.tensors[st.b].batched ? 1048576.0 : 1.0, (int)st.free_b.size());
+      st.double_a = wa < wb;
+    }
     auto operand = [&](int t, const std::vector<int>& fr) {
       TnOperand o;
       o.tensor = t;
+      o.doubled = (t == st.a) == st.double_a;
       o.nf = (int)fr.size();
       o.nc = (int)st.contracted.size();
       const TnTensor& T = net.tensors[t];
@@ -554,10 +562,11 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
       (T.batched ? ab : au).release(T.arena, inter_reals(T));
     }
     TnTensor out;
-    out.idx = st.free_a;
-    out.idx.insert(out.idx.end(), st.free_b.begin(), st.free_b.end());
+    out.idx = st.free_b;
+    out.idx.insert(out.idx.end(), st.free_a.begin(), st.free_a.end());
     out.lm = (int)st.free_a.size();
     out.ln = (int)st.free_b.size();
+    out.split = st.double_a;
     out.batched = st.batched;
     out.arena = (out.batched ? ab : au).alloc(inter_reals(out));
     st.out = (int)net.tensors.size();
@@ -576,7 +585,8 @@ int64_t tn_scratch_reals(const TnNet& net, int64_t batch) {
   int64_t m = 0;
   for (const TnStep& s : net.steps) {
     int64_t ba = net.tensors[s.a].batched ? batch : 1, bb = net.tensors[s.b].batched ? batch : 1;
-    int64_t v = (2ll << (s.opa.nf + s.opa.nc)) * ba + (2ll << (s.opb.nf + s.opb.nc)) * bb;
+    int64_t v = ((s.opa.doubled ? 4ll : 2ll) << (s.opa.nf + s.opa.nc)) * ba +
+                ((s.opb.doubled ? 4ll : 2ll) << (s.opb.nf + s.opb.nc)) * bb;
     m = std::max(m, v);
   }
   return m;
@@ -591,7 +601,8 @@ static void ints(std::ostringstream& o, const std::vector<int>& v) {
 }
 
 static void operand_json(std::ostringstream& o, const TnOperand& x) {
-  o << "{\"tensor\":" << x.tensor << ",\"nf\":" << x.nf << ",\"nc\":" << x.nc << ",\"src_bit\":";
+  o << "{\"tensor\":" << x.tensor << ",\"nf\":" << x.nf << ",\"nc\":" << x.nc
+    << ",\"doubled\":" << (x.doubled ? 1 : 0) << ",\"src_bit\":";
   ints(o, x.src_bit);
   o << ",\"slice_bit\":[";
   for (size_t i = 0; i < x.slice_bit.size(); ++i)
@@ -626,7 +637,8 @@ std::string tn_describe(const std::vector<TnNet>& nets, int n_params, int precis
     for (size_t i = 0; i < n.tensors.size(); ++i) {
       const TnTensor& t = n.tensors[i];
       o << (i ? "," : "") << "{\"leaf\":" << t.leaf << ",\"gate\":" << t.gate << ",\"batched\":" << (t.batched ? 1 : 0)
-        << ",\"lm\":" << t.lm << ",\"ln\":" << t.ln << ",\"off\":" << t.off << ",\"arena\":" << t.arena
+        << ",\"lm\":" << t.lm << ",\"ln\":" << t.ln << ",\"split\":" << (t.split ? 1 : 0) << ",\"off\":" << t.off
+        << ",\"arena\":" << t.arena
         << ",\"full_idx\":";
       ints(o, t.full_idx);
       o << ",\"idx\":";
@@ -637,7 +649,7 @@ std::string tn_describe(const std::vector<TnNet>& nets, int n_params, int precis
     for (size_t i = 0; i < n.steps.size(); ++i) {
       const TnStep& s = n.steps[i];
       o << (i ? "," : "") << "{\"a\":" << s.a << ",\"b\":" << s.b << ",\"out\":" << s.out
-        << ",\"batched\":" << (s.batched ? 1 : 0) << ",\"opa\":";
+        << ",\"batched\":" << (s.batched ? 1 : 0) << ",\"double_a\":" << (s.double_a ? 1 : 0) << ",\"opa\":";
       operand_json(o, s.opa);
       o << ",\"opb\":";
       operand_json(o, s.opb);

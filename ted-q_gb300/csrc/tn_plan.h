@@ -20,11 +20,14 @@
 // Storage of a tensor with index list L (rank r): element at flat index
 // sum_t bit_t << (r-1-t), i.e. L[0] is the most significant bit.
 //  * leaves: interleaved complex;
-//  * intermediates (product of step s with free_a, free_b): the real product
-//    P (2M x 2N, column-major, M = 2^|free_a|, N = 2^|free_b|) of the planar
-//    operands [Re A; Im A] (2M x K) and [Re B, Im B] (K x 2N); element (i, j)
-//    of the complex result is (P(i,j) - P(M+i,N+j), P(i,N+j) + P(M+i,j)), and
-//    its index list is free_a ++ free_b.
+//  * intermediates: the result C (M x N, M = 2^|free_a|, N = 2^|free_b|) of
+//    one real GEMM over the real embedding of the complex product -- either
+//    [Re A, Im A] (M x 2K) x [[Re B, Im B], [-Im B, Re B]] (2K x 2N) = [Re C, Im C]
+//    ("planar": Re C(i,j) at j*M + i, Im C at + M*N), or
+//    [[Re A, -Im A], [Im A, Re A]] (2M x 2K) x [Re B; Im B] (2K x N) = [Re C; Im C]
+//    ("split": Re C(i,j) at j*2M + i, Im C at + M).  The operand with the
+//    smaller free dimension is the doubled one.  Index list: free_b ++ free_a
+//    (i is the low part of the flat index).
 #pragma once
 #include <stdint.h>
 
@@ -44,6 +47,7 @@ struct TnTensor {
   int gate = -1;              // TL_GATE / TL_GATE_CONJ: index into TnNet::gates
   bool batched = false;       // depends on the parameters
   int lm = 0, ln = 0;         // intermediates: |free_a|, |free_b| of the producing step
+  bool split = false;         // intermediates: "split" layout (else "planar")
   // leaves: offset of the stored tensor (complex elements); batched leaves in
   // the per-call batched-leaf region (times the batch), the others in the
   // plan's constant buffer
@@ -61,12 +65,15 @@ struct TnGate {
   std::vector<double> fixed;  // !param: 2 * 4^k doubles (re, im), row-major
 };
 
-// Gather of one GEMM operand: output element e of [F][K] (K = 2^nc) takes
-// source bit src_bit[o] for output bit o (o = 0 least significant); leaf
-// operands with sliced indices add slice_bit[q] when sliced index q is 1.
+// Gather of one GEMM operand: element e = f*K + k (K = 2^nc) takes source bit
+// src_bit[o] for bit o of e (o = 0 least significant); leaf operands with
+// sliced indices add slice_bit[q] when sliced index q is 1.  Rows of 2K reals:
+// [Re(f,:), Im(f,:)], and for the doubled operand F more rows
+// [Im(f,:), Re(f,:)] after rows [Re(f,:), -Im(f,:)].
 struct TnOperand {
   int tensor = -1;
   int nf = 0, nc = 0;
+  bool doubled = false;
   std::vector<int> src_bit;
   std::vector<std::pair<int, int>> slice_bit;  // (sliced index number, source bit)
 };
@@ -76,6 +83,7 @@ struct TnStep {
   std::vector<int> free_a, free_b, contracted;
   TnOperand opa, opb;
   bool batched = false;
+  bool double_a = false;  // A is the doubled operand (result in "split" layout)
 };
 
 struct TnNet {

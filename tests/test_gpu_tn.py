@@ -20,7 +20,8 @@ qai = pytest.importorskip("tedq_gb300")
 from tedq_gb300.templates import hea_spec, lattice_spec  # noqa: E402
 
 DEV = "cuda:0"
-TOL = {("c64", "bf16x9"): 1e-5, ("c64", "fp32"): 1e-5, ("c64", "tf32"): 5e-3, ("c128", "bf16x9"): 1e-12}
+TOL = {("c64", "bf16x9"): 1e-5, ("c64", "fp32"): 1e-5, ("c64", "auto"): 1e-5, ("c64", "tf32"): 5e-3,
+       ("c128", "bf16x9"): 1e-12}
 
 
 def _tn(spec, precision="c64", gemm="bf16x9", **kw):
@@ -38,8 +39,9 @@ def _native_loaded():
     assert qai._lib._lib is not None, "native library was not used"
 
 
-@pytest.mark.parametrize("mode", [("c64", "bf16x9"), ("c64", "fp32"), ("c64", "tf32"), ("c128", "bf16x9")],
-                         ids=["c64-bf16x9", "c64-fp32", "c64-tf32", "c128"])
+@pytest.mark.parametrize("mode", [("c64", "bf16x9"), ("c64", "fp32"), ("c64", "auto"), ("c64", "tf32"),
+                                  ("c128", "bf16x9")],
+                         ids=["c64-bf16x9", "c64-fp32", "c64-auto", "c64-tf32", "c128"])
 @pytest.mark.parametrize("seed", range(6))
 def test_tn_random_circuits(seed, mode):
     precision, gemm = mode

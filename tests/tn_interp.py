@@ -1,10 +1,11 @@
 """NumPy executor of an exported tensor-network plan (``tedq_tn_plan_describe``).
 
 Runs exactly what the device runs -- per step the two bit-permutation gathers
-into planar real operands (with the complex combination of a producer's real
-product), one real GEMM [Re A; Im A] (2M x K) x [Re B, Im B]^T (K x 2N), and the
-root value P(0,0) - P(1,1) summed over slices -- in float64, so the plan's
-index maps, slicing offsets and 4M block layout are checked on the CPU.
+into rows of real GEMM operands (the operand with the smaller free dimension
+in the doubled [[Re, -Im], [Im, Re]] form of the real embedding), one real GEMM
+whose column-major result holds Re C and Im C ("planar" or "split" layout), and
+the root's real part summed over slices -- in float64, so the plan's index
+maps, slicing offsets and GEMM layouts are checked on the CPU.
 Parameter-dependent gate tensors come from the oracle's gate definitions.
 """
 
@@ -50,11 +51,15 @@ def _gather(net, op, store, sl):
         vals = src[flat]
     else:
         M, N = 1 << T["lm"], 1 << T["ln"]
-        i, j = flat >> T["ln"], flat & (N - 1)
-        vals = (src[i, j] - src[M + i, N + j]) + 1j * (src[i, N + j] + src[M + i, j])
+        i, j = flat & (M - 1), flat >> T["lm"]
+        sj, sp = (2 * M, M) if T["split"] else (M, M * N)
+        vals = src[j * sj + i] + 1j * src[j * sj + i + sp]
     F, K = 1 << op["nf"], 1 << op["nc"]
     v = vals.reshape(F, K)
-    return np.concatenate([v.real, v.imag], axis=0)  # [2F, K]
+    rows = np.concatenate([v.real, v.imag], axis=1)  # [F, 2K]
+    if op["doubled"]:
+        rows = np.concatenate([np.concatenate([v.real, -v.imag], axis=1), np.concatenate([v.imag, v.real], axis=1)])
+    return rows
 
 
 def run_net(net, prm):
@@ -64,11 +69,10 @@ def run_net(net, prm):
     for sl in range(1 << len(net["sliced"])):
         store = dict(leaves)
         for st in net["steps"]:
-            A = _gather(net, st["opa"], store, sl)
-            B = _gather(net, st["opb"], store, sl)
-            store[st["out"]] = A @ B.T  # P: [2M, 2N]
-        P = store[net["root"]]
-        total += P[0, 0] - P[1, 1]
+            A = _gather(net, st["opa"], store, sl)  # rows of op(A)
+            B = _gather(net, st["opb"], store, sl)  # columns of B
+            store[st["out"]] = (A @ B.T).reshape(-1, order="F")  # column-major result
+        total += store[net["root"]][0]
     return total
 
 
@@ -87,7 +91,7 @@ def check_arenas(net):
             if t >= L:
                 live.pop(t)
         o = st["out"]
-        size = 4 << (T[o]["lm"] + T[o]["ln"])
+        size = 2 << (T[o]["lm"] + T[o]["ln"])
         lo, hi = T[o]["arena"], T[o]["arena"] + size
         arena_max = net["batched_arena"] if T[o]["batched"] else net["unbatched_arena"]
         assert 0 <= lo and hi <= arena_max
