@@ -296,10 +296,10 @@ typedef struct tedq_tn_plan tedq_tn_plan_t;
 
 /* GEMM arithmetic of the complex64 mode (complex128 uses FP64 GEMMs). */
 enum {
-  TEDQ_TN_GEMM_BF16X9 = 0,  /* FP32 accuracy from BF16 tensor-core products
+  TEDQ_TN_GEMM_FP32 = 0,    /* FP32 (default)                                 */
+  TEDQ_TN_GEMM_BF16X9 = 1,  /* FP32 accuracy from BF16 tensor-core products
                                (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9)    */
-  TEDQ_TN_GEMM_TF32 = 1,    /* one TF32 product per term (~1e-3 relative)     */
-  TEDQ_TN_GEMM_FP32 = 2,    /* FP32 without tensor cores                      */
+  TEDQ_TN_GEMM_TF32 = 2,    /* one TF32 product per term (~1e-3 relative)     */
   TEDQ_TN_GEMM_AUTO = 3     /* BF16x9 where cuBLAS's heuristics expect it to be
                                faster than FP32, FP32 elsewhere (same accuracy) */
 };

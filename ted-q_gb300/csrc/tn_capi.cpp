@@ -111,7 +111,7 @@ struct TnDevice {
 
 struct tedq_tn_plan {
   std::vector<TnNet> nets;
-  int n = 0, n_params = 0, precision = TEDQ_PREC_C64, gemm = TEDQ_TN_GEMM_BF16X9;
+  int n = 0, n_params = 0, precision = TEDQ_PREC_C64, gemm = TEDQ_TN_GEMM_FP32;
   bool graphs = false;
   std::vector<std::vector<TnLeafDesc>> descs;
   std::vector<int64_t> const_base;  // reals, per network
@@ -423,7 +423,7 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
     if (opts) {
       if (opts->precision != TEDQ_PREC_C64 && opts->precision != TEDQ_PREC_C128)
         throw std::invalid_argument("unknown precision");
-      if (opts->gemm < TEDQ_TN_GEMM_BF16X9 || opts->gemm > TEDQ_TN_GEMM_AUTO)
+      if (opts->gemm < TEDQ_TN_GEMM_FP32 || opts->gemm > TEDQ_TN_GEMM_AUTO)
         throw std::invalid_argument("unknown GEMM mode");
       if (opts->max_rank < 0 || opts->max_rank > 34) throw std::invalid_argument("max_rank out of range");
       p->precision = opts->precision;

@@ -97,7 +97,7 @@ class TnProfile(ctypes.Structure):
                 ("reserved", c_int64 * 4)]
 
 
-TN_GEMM = {"bf16x9": 0, "tf32": 1, "fp32": 2, "auto": 3}
+TN_GEMM = {"fp32": 0, "bf16x9": 1, "tf32": 2, "auto": 3}
 
 # every symbol the header declares, with (restype, argtypes)
 SIGNATURES = {

@@ -24,7 +24,7 @@ TOL = {("c64", "bf16x9"): 1e-5, ("c64", "fp32"): 1e-5, ("c64", "auto"): 1e-5, ("
        ("c128", "bf16x9"): 1e-12}
 
 
-def _tn(spec, precision="c64", gemm="bf16x9", **kw):
+def _tn(spec, precision="c64", gemm="fp32", **kw):
     return qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, precision=precision,
                                                       tn_gemm=gemm, **kw)
 
@@ -128,7 +128,7 @@ def test_tn_workspace_and_errors():
     spec = random_spec(2)
     cc = _tn(spec, requires_grad=False)
     prog = cc._prog
-    assert prog.workspace_bytes(4) > prog.workspace_bytes(1)
+    assert prog.workspace_bytes(4096) > prog.workspace_bytes(1)
     P = torch.zeros((1, prog.n_params + 1), device=DEV)
     with pytest.raises(ValueError):
         cc.execute_batch(P)
