@@ -507,7 +507,7 @@ def run_tn(a):
     B = a.batch
     t_plan = time.perf_counter()
     cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, tn_gemm=a.tn_gemm,
-                                                    tn_graphs=True, requires_grad=False)
+                                                    tn_graphs=bool(a.tn_graphs), requires_grad=False)
     t_plan = time.perf_counter() - t_plan
     info = cc.program_info
     P = info["n_params"]
@@ -525,11 +525,12 @@ def run_tn(a):
                                       ctypes.c_void_p(outs[i].data_ptr()), ctypes.c_void_p(ws), wsb,
                                       ctypes.c_void_p(stream.cuda_stream)), "tedq_tn_contract")
 
-    # every timed step uses its own parameter and output buffers: capture each
-    # graph during warm-up (two calls per buffer set: eager, then captured)
+    # every timed step uses its own parameter and output buffers; with graphs,
+    # capture each one during warm-up (two calls per buffer set: eager, captured)
     for i in range(a.warmup + a.steps):
         step(i)
-        step(i)
+        if a.tn_graphs:
+            step(i)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
@@ -601,7 +602,7 @@ def run_tn(a):
                        "params_per_circuit": P, "contractions_per_circuit": info["n_steps"],
                        "largest_intermediate_log2": info["max_rank"], "sliced": info["n_sliced"],
                        "flops_per_circuit": 2.0 ** info["log2_flops"], "batch_per_gpu": B,
-                       "plan_s": round(t_plan, 3), "graphs": True,
+                       "plan_s": round(t_plan, 3), "graphs": bool(a.tn_graphs),
                        "l2": "inputs larger than L2 (intermediates %.1f GB per step)" %
                              (prog.workspace_bytes(B) / 1e9)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4, "d2h_bytes_per_step": B * 4},
@@ -641,6 +642,7 @@ def main():
     ap.add_argument("--workload", default="vqc", choices=["vqc", "serving", "tn"])
     ap.add_argument("--tn-gemm", default="fp32", choices=["bf16x9", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
+    ap.add_argument("--tn-graphs", type=int, default=0, help="replay each call as a CUDA graph")
     ap.add_argument("--rates", default="100,500,2000,5000")
     ap.add_argument("--duration", type=float, default=2.0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
