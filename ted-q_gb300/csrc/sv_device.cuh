@@ -90,6 +90,105 @@ __device__ __forceinline__ real recb(cpx<real> a, cpx<real> b) {
   return a.x * b.x + a.y * b.y;
 }
 
+// ---------------------------------------------------------------- register sets
+// A thread's 2^R amplitudes of a phase.  complex128: one cpx per amplitude.
+// complex64: amplitudes 2g and 2g+1 (register bit 0 is the "pair bit") are
+// packed per group g as float2 (re_2g, re_2g+1) and (im_2g, im_2g+1), so one
+// packed FP32x2 instruction (FFMA2) updates two amplitudes.
+template <typename real, int R>
+struct Regs;
+template <int R>
+struct Regs<double, R> {
+  cpx<double> a[1 << R];
+};
+template <int R>
+struct Regs<float, R> {
+  float2 re[1 << (R - 1)], im[1 << (R - 1)];
+};
+
+// Shared-memory image of a 16-byte unit: complex64 units hold their two
+// amplitudes pair-planar (re0, re1, im0, im1), complex128 units one amplitude.
+template <typename real>
+struct SUnit;
+template <>
+struct alignas(16) SUnit<float> {
+  float2 re, im;
+};
+template <>
+struct alignas(16) SUnit<double> {
+  cpx<double> v;
+};
+
+__device__ __forceinline__ SUnit<float> to_s(const Unit<float>& u) {
+  SUnit<float> s;
+  s.re = make_float2(u.v[0].x, u.v[1].x);
+  s.im = make_float2(u.v[0].y, u.v[1].y);
+  return s;
+}
+__device__ __forceinline__ Unit<float> from_s(const SUnit<float>& s) {
+  Unit<float> u;
+  u.v[0] = mk<float>(s.re.x, s.im.x);
+  u.v[1] = mk<float>(s.re.y, s.im.y);
+  return u;
+}
+__device__ __forceinline__ SUnit<double> to_s(const Unit<double>& u) {
+  SUnit<double> s;
+  s.v = u.v[0];
+  return s;
+}
+__device__ __forceinline__ Unit<double> from_s(const SUnit<double>& s) {
+  Unit<double> u;
+  u.v[0] = s.v;
+  return u;
+}
+
+// Amplitude `addr` (unit << E | amplitude-in-unit) of a shared-memory image.
+__device__ __forceinline__ cpx<float> amp_ld(const SUnit<float>* t, uint32_t addr) {
+  const float* f = reinterpret_cast<const float*>(t + (addr >> 1));
+  return mk<float>(f[addr & 1], f[2 + (addr & 1)]);
+}
+__device__ __forceinline__ void amp_st(SUnit<float>* t, uint32_t addr, cpx<float> v) {
+  float* f = reinterpret_cast<float*>(t + (addr >> 1));
+  f[addr & 1] = v.x;
+  f[2 + (addr & 1)] = v.y;
+}
+__device__ __forceinline__ cpx<double> amp_ld(const SUnit<double>* t, uint32_t addr) { return t[addr].v; }
+__device__ __forceinline__ void amp_st(SUnit<double>* t, uint32_t addr, cpx<double> v) { t[addr].v = v; }
+
+// unit j of a register set <-> shared-memory unit
+template <int R>
+__device__ __forceinline__ void regs_ld(Regs<float, R>& A, int j, const SUnit<float>& s) {
+  A.re[j] = s.re;
+  A.im[j] = s.im;
+}
+template <int R>
+__device__ __forceinline__ SUnit<float> regs_st(const Regs<float, R>& A, int j) {
+  SUnit<float> s;
+  s.re = A.re[j];
+  s.im = A.im[j];
+  return s;
+}
+template <int R>
+__device__ __forceinline__ void regs_ld(Regs<double, R>& A, int j, const SUnit<double>& s) {
+  A.a[j] = s.v;
+}
+template <int R>
+__device__ __forceinline__ SUnit<double> regs_st(const Regs<double, R>& A, int j) {
+  SUnit<double> s;
+  s.v = A.a[j];
+  return s;
+}
+
+// packed FP32x2 helpers
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 swp(float2 a) { return make_float2(a.y, a.x); }
+// a gate controlled on the pair bit changes only the odd half
+__device__ __forceinline__ float2 odd_only(bool c0, float2 old, float2 nw) {
+  return c0 ? make_float2(old.x, nw.y) : nw;
+}
+
 __device__ __forceinline__ void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
 __device__ __forceinline__ void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
 
@@ -198,11 +297,11 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
 }
 
 // ---------------------------------------------------------------- register gates
-// a[2^R]: the thread's amplitudes; bit k of the register index is register
-// bit k.  Ctl is an unsigned run-time mask or a CM<> constant.
+// Complex-array forms (complex128 register sets): bit k of the register index
+// is register bit k.  Ctl is an unsigned run-time mask or a CM<> constant.
 
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_u1(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+__device__ __forceinline__ void apply_u1_c(cpx<real>* a, const cpx<real>* M, Ctl cm) {
   const cpx<real> m0 = M[0], m1 = M[1], m2 = M[2], m3 = M[3];
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -216,7 +315,7 @@ __device__ __forceinline__ void apply_u1(cpx<real>* a, const cpx<real>* M, Ctl c
 }
 
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_d1(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+__device__ __forceinline__ void apply_d1_c(cpx<real>* a, const cpx<real>* M, Ctl cm) {
   const cpx<real> d0 = M[0], d1 = M[1];
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -227,7 +326,7 @@ __device__ __forceinline__ void apply_d1(cpx<real>* a, const cpx<real>* M, Ctl c
 
 // RX-type [[c, -i s], [-i s, c]] (RX, or RX^dagger with s negated)
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_rxt(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+__device__ __forceinline__ void apply_rxt_c(cpx<real>* a, const cpx<real>* M, Ctl cm) {
   const real c = M[0].x, sn = -M[1].y;
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -242,7 +341,7 @@ __device__ __forceinline__ void apply_rxt(cpx<real>* a, const cpx<real>* M, Ctl 
 
 // RY-type [[c, -s], [s, c]]
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_ryt(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+__device__ __forceinline__ void apply_ryt_c(cpx<real>* a, const cpx<real>* M, Ctl cm) {
   const real c = M[0].x, sn = -M[1].x;
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -257,7 +356,7 @@ __device__ __forceinline__ void apply_ryt(cpx<real>* a, const cpx<real>* M, Ctl 
 
 // diag(1, d): multiply the |1> half only
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_ph(cpx<real>* a, const cpx<real>* M, Ctl cm) {
+__device__ __forceinline__ void apply_ph_c(cpx<real>* a, const cpx<real>* M, Ctl cm) {
   const cpx<real> d = M[1];
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -268,7 +367,7 @@ __device__ __forceinline__ void apply_ph(cpx<real>* a, const cpx<real>* M, Ctl c
 }
 
 template <int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ void apply_x(cpx<real>* a, Ctl cm) {
+__device__ __forceinline__ void apply_x_c(cpx<real>* a, Ctl cm) {
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
     if (i & (1 << K)) continue;
@@ -283,7 +382,7 @@ __device__ __forceinline__ void apply_x(cpx<real>* a, Ctl cm) {
 // Per-thread part of Im <lambda| G |psi> on the control subspace
 // (G = X, Y, Z or P1 = |1><1| on register bit K).
 template <int G, int K, int R, typename real, typename Ctl>
-__device__ __forceinline__ real grad_part(const cpx<real>* p, const cpx<real>* l, Ctl cm) {
+__device__ __forceinline__ real grad_part_c(const cpx<real>* p, const cpx<real>* l, Ctl cm) {
   real acc = 0;
 #pragma unroll
   for (int i = 0; i < (1 << R); ++i) {
@@ -298,10 +397,279 @@ __device__ __forceinline__ real grad_part(const cpx<real>* p, const cpx<real>* l
   return acc;
 }
 
+// complex128 register sets
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_u1(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
+  apply_u1_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_d1(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
+  apply_d1_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_rxt(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
+  apply_rxt_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ryt(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
+  apply_ryt_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ph(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
+  apply_ph_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_x(Regs<double, R>& A, Ctl cm) {
+  apply_x_c<K, R, double>(A.a, cm);
+}
+template <int G, int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ double grad_part(const Regs<double, R>& p, const Regs<double, R>& l, Ctl cm) {
+  return grad_part_c<G, K, R, double>(p.a, l.a, cm);
+}
+
+// complex64 register sets (packed pairs): group g holds amplitudes 2g and
+// 2g+1; a gate on register bit K >= 1 pairs group g with g | 1 << (K-1) and
+// runs on FP32x2 instructions; a gate on bit 0 mixes the halves of a group.
+// A control on bit 0 restricts a gate to the odd halves.
+#define TEDQ_GROUPS                                  \
+  constexpr int NG = 1 << (R - 1);                   \
+  const unsigned cg = (unsigned)cm >> 1;             \
+  const bool c0 = ((unsigned)cm & 1u) != 0u;         \
+  (void)c0;
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_u1(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
+  TEDQ_GROUPS
+  if constexpr (K == 0) {
+    const cpx<float> m0 = M[0], m1 = M[1], m2 = M[2], m3 = M[3];
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if ((g & cg) != cg) continue;
+      const cpx<float> x0 = mk<float>(A.re[g].x, A.im[g].x), x1 = mk<float>(A.re[g].y, A.im[g].y);
+      const cpx<float> y0 = cmac2(m0, x0, m1, x1), y1 = cmac2(m2, x0, m3, x1);
+      A.re[g] = make_float2(y0.x, y1.x);
+      A.im[g] = make_float2(y0.y, y1.y);
+    }
+  } else {
+    const float2 m0r = bc2(M[0].x), m0i = bc2(M[0].y), n0i = bc2(-M[0].y);
+    const float2 m1r = bc2(M[1].x), m1i = bc2(M[1].y), n1i = bc2(-M[1].y);
+    const float2 m2r = bc2(M[2].x), m2i = bc2(M[2].y), n2i = bc2(-M[2].y);
+    const float2 m3r = bc2(M[3].x), m3i = bc2(M[3].y), n3i = bc2(-M[3].y);
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if (g & (1 << (K - 1))) continue;
+      if ((g & cg) != cg) continue;
+      const int h = g | (1 << (K - 1));
+      const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+      float2 yr0 = mul2(m0r, xr0);
+      yr0 = fma2(n0i, xi0, yr0);
+      yr0 = fma2(m1r, xr1, yr0);
+      yr0 = fma2(n1i, xi1, yr0);
+      float2 yi0 = mul2(m0r, xi0);
+      yi0 = fma2(m0i, xr0, yi0);
+      yi0 = fma2(m1r, xi1, yi0);
+      yi0 = fma2(m1i, xr1, yi0);
+      float2 yr1 = mul2(m2r, xr0);
+      yr1 = fma2(n2i, xi0, yr1);
+      yr1 = fma2(m3r, xr1, yr1);
+      yr1 = fma2(n3i, xi1, yr1);
+      float2 yi1 = mul2(m2r, xi0);
+      yi1 = fma2(m2i, xr0, yi1);
+      yi1 = fma2(m3r, xi1, yi1);
+      yi1 = fma2(m3i, xr1, yi1);
+      A.re[g] = odd_only(c0, xr0, yr0);
+      A.im[g] = odd_only(c0, xi0, yi0);
+      A.re[h] = odd_only(c0, xr1, yr1);
+      A.im[h] = odd_only(c0, xi1, yi1);
+    }
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_d1(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
+  TEDQ_GROUPS
+  float2 dr0, di0, dr1, di1;  // multipliers of a group whose bit K-1 is 0 / 1
+  if constexpr (K == 0) {
+    dr0 = dr1 = make_float2(M[0].x, M[1].x);
+    di0 = di1 = make_float2(M[0].y, M[1].y);
+  } else {
+    dr0 = bc2(M[0].x);
+    di0 = bc2(M[0].y);
+    dr1 = bc2(M[1].x);
+    di1 = bc2(M[1].y);
+  }
+  const float2 nd0 = make_float2(-di0.x, -di0.y), nd1 = make_float2(-di1.x, -di1.y);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    if ((g & cg) != cg) continue;
+    const bool hi = K > 0 && ((g >> (K > 0 ? K - 1 : 0)) & 1);
+    const float2 dr = hi ? dr1 : dr0, di = hi ? di1 : di0, nd = hi ? nd1 : nd0;
+    const float2 xr = A.re[g], xi = A.im[g];
+    const float2 yr = fma2(nd, xi, mul2(dr, xr));
+    const float2 yi = fma2(di, xr, mul2(dr, xi));
+    A.re[g] = odd_only(c0, xr, yr);
+    A.im[g] = odd_only(c0, xi, yi);
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_rxt(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
+  TEDQ_GROUPS
+  const float2 C = bc2(M[0].x), S = bc2(-M[1].y), NS = bc2(M[1].y);
+  if constexpr (K == 0) {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if ((g & cg) != cg) continue;
+      const float2 xr = A.re[g], xi = A.im[g];
+      A.re[g] = fma2(C, xr, mul2(S, swp(xi)));
+      A.im[g] = fma2(C, xi, mul2(NS, swp(xr)));
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if (g & (1 << (K - 1))) continue;
+      if ((g & cg) != cg) continue;
+      const int h = g | (1 << (K - 1));
+      const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+      A.re[g] = odd_only(c0, xr0, fma2(C, xr0, mul2(S, xi1)));
+      A.im[g] = odd_only(c0, xi0, fma2(C, xi0, mul2(NS, xr1)));
+      A.re[h] = odd_only(c0, xr1, fma2(C, xr1, mul2(S, xi0)));
+      A.im[h] = odd_only(c0, xi1, fma2(C, xi1, mul2(NS, xr0)));
+    }
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ryt(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
+  TEDQ_GROUPS
+  const float c = M[0].x, sn = -M[1].x;
+  const float2 C = bc2(c), S = bc2(sn), NS = bc2(-sn);
+  if constexpr (K == 0) {
+    const float2 W = make_float2(-sn, sn);
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if ((g & cg) != cg) continue;
+      const float2 xr = A.re[g], xi = A.im[g];
+      A.re[g] = fma2(C, xr, mul2(W, swp(xr)));
+      A.im[g] = fma2(C, xi, mul2(W, swp(xi)));
+    }
+  } else {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if (g & (1 << (K - 1))) continue;
+      if ((g & cg) != cg) continue;
+      const int h = g | (1 << (K - 1));
+      const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+      A.re[g] = odd_only(c0, xr0, fma2(C, xr0, mul2(NS, xr1)));
+      A.im[g] = odd_only(c0, xi0, fma2(C, xi0, mul2(NS, xi1)));
+      A.re[h] = odd_only(c0, xr1, fma2(S, xr0, mul2(C, xr1)));
+      A.im[h] = odd_only(c0, xi1, fma2(S, xi0, mul2(C, xi1)));
+    }
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_ph(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
+  TEDQ_GROUPS
+  float2 dr, di;
+  if constexpr (K == 0) {
+    dr = make_float2(1.f, M[1].x);
+    di = make_float2(0.f, M[1].y);
+  } else {
+    dr = bc2(M[1].x);
+    di = bc2(M[1].y);
+  }
+  const float2 nd = make_float2(-di.x, -di.y);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    if (K > 0 && !((g >> (K > 0 ? K - 1 : 0)) & 1)) continue;
+    if ((g & cg) != cg) continue;
+    const float2 xr = A.re[g], xi = A.im[g];
+    A.re[g] = odd_only(c0, xr, fma2(nd, xi, mul2(dr, xr)));
+    A.im[g] = odd_only(c0, xi, fma2(di, xr, mul2(dr, xi)));
+  }
+}
+
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_x(Regs<float, R>& A, Ctl cm) {
+  TEDQ_GROUPS
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    if ((g & cg) != cg) continue;
+    if constexpr (K == 0) {
+      A.re[g] = swp(A.re[g]);
+      A.im[g] = swp(A.im[g]);
+    } else {
+      if (g & (1 << (K - 1))) continue;
+      const int h = g | (1 << (K - 1));
+      const float2 r0 = A.re[g], i0 = A.im[g], r1 = A.re[h], i1 = A.im[h];
+      A.re[g] = odd_only(c0, r0, r1);
+      A.im[g] = odd_only(c0, i0, i1);
+      A.re[h] = odd_only(c0, r1, r0);
+      A.im[h] = odd_only(c0, i1, i0);
+    }
+  }
+}
+
+template <int G, int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ float grad_part(const Regs<float, R>& p, const Regs<float, R>& l, Ctl cm) {
+  TEDQ_GROUPS
+  float2 ap = make_float2(0.f, 0.f), an = make_float2(0.f, 0.f);
+  if constexpr (K == 0) {
+    float acc = 0.f;
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if ((g & cg) != cg) continue;
+      const float2 pr = p.re[g], pi = p.im[g], lr = l.re[g], li = l.im[g];
+      if (G == GR_X) acc += (lr.x * pi.y - li.x * pr.y) + (lr.y * pi.x - li.y * pr.x);
+      if (G == GR_Y) acc += (lr.y * pr.x + li.y * pi.x) - (lr.x * pr.y + li.x * pi.y);
+      if (G == GR_Z || G == GR_P1) {
+        ap = fma2(lr, pi, ap);
+        an = fma2(li, pr, an);
+      }
+    }
+    if (G == GR_Z) acc += (ap.x - an.x) - (ap.y - an.y);
+    if (G == GR_P1) acc += ap.y - an.y;
+    return acc;
+  } else {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if (g & (1 << (K - 1))) continue;
+      if ((g & cg) != cg) continue;
+      const int h = g | (1 << (K - 1));
+      if (G == GR_X) {
+        ap = fma2(l.re[g], p.im[h], ap);
+        an = fma2(l.im[g], p.re[h], an);
+        ap = fma2(l.re[h], p.im[g], ap);
+        an = fma2(l.im[h], p.re[g], an);
+      }
+      if (G == GR_Y) {
+        ap = fma2(l.re[h], p.re[g], ap);
+        ap = fma2(l.im[h], p.im[g], ap);
+        an = fma2(l.re[g], p.re[h], an);
+        an = fma2(l.im[g], p.im[h], an);
+      }
+      if (G == GR_Z) {
+        ap = fma2(l.re[g], p.im[g], ap);
+        an = fma2(l.im[g], p.re[g], an);
+        an = fma2(l.re[h], p.im[h], an);
+        ap = fma2(l.im[h], p.re[h], ap);
+      }
+      if (G == GR_P1) {
+        ap = fma2(l.re[h], p.im[h], ap);
+        an = fma2(l.im[h], p.re[h], an);
+      }
+    }
+    const float dx = ap.x - an.x, dy = ap.y - an.y;
+    return c0 ? dy : dx + dy;
+  }
+}
+#undef TEDQ_GROUPS
+
 // ---------------------------------------------------------------- run-time dispatch
 
 template <int R, typename real, int K = 0>
-__device__ __forceinline__ void dispatch_gate(int kind, int k, cpx<real>* a, const cpx<real>* M, unsigned cm) {
+__device__ __forceinline__ void dispatch_gate(int kind, int k, Regs<real, R>& a, const cpx<real>* M, unsigned cm) {
   if constexpr (K < R) {
     if (k == K) {
       switch (kind) {
@@ -319,7 +687,7 @@ __device__ __forceinline__ void dispatch_gate(int kind, int k, cpx<real>* a, con
 }
 
 template <int R, typename real>
-__device__ __forceinline__ void apply_rgate(const RGate& r, cpx<real>* a, const cpx<real>* M) {
+__device__ __forceinline__ void apply_rgate(const RGate& r, Regs<real, R>& a, const cpx<real>* M) {
   if (r.kind == GK_SWAP) {
     const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
     dispatch_gate<R, real>(GK_X, r.k1, a, M, r.cmask | b0);
@@ -331,7 +699,8 @@ __device__ __forceinline__ void apply_rgate(const RGate& r, cpx<real>* a, const 
 }
 
 template <int R, typename real, int K = 0>
-__device__ __forceinline__ real dispatch_grad(int g, int k, const cpx<real>* p, const cpx<real>* l, unsigned cm) {
+__device__ __forceinline__ real dispatch_grad(int g, int k, const Regs<real, R>& p, const Regs<real, R>& l,
+                                              unsigned cm) {
   if constexpr (K < R) {
     if (k == K) {
       switch (g) {
@@ -380,9 +749,8 @@ __device__ __forceinline__ Unit<real> load_unit(const PassParams& P, const cpx<r
 
 // Dense fixed k-qubit matrix applied directly on the shared-memory tile.
 template <typename real>
-__device__ void dense_phase(const PassParams& P, const Phase& ph, Unit<real>* tile, int tid, int T) {
+__device__ void dense_phase(const PassParams& P, const Phase& ph, SUnit<real>* tile, int tid, int T) {
   constexpr int E = UnitsPerAmp<real>::E;
-  cpx<real>* amp = reinterpret_cast<cpx<real>*>(tile);
   const int k = ph.dk, d = 1 << k;
   uint32_t dmask = 0;
   for (int i = 0; i < k; ++i) dmask |= 1u << ph.dpos[i];
@@ -404,7 +772,7 @@ __device__ void dense_phase(const PassParams& P, const Phase& ph, Unit<real>* ti
         for (int i = 0; i < k; ++i)
           if ((r >> (k - 1 - i)) & 1) t |= 1u << ph.dpos[i];
         addr[r] = (swz_unit(t >> E) << E) | (t & ((1u << E) - 1));
-        v[r] = amp[addr[r]];
+        v[r] = amp_ld(tile, addr[r]);
       }
     }
 #pragma unroll
@@ -426,7 +794,7 @@ __device__ void dense_phase(const PassParams& P, const Phase& ph, Unit<real>* ti
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r)
-      if (r < d) amp[addr[r]] = w[r];
+      if (r < d) amp_st(tile, addr[r], w[r]);
   }
 }
 
@@ -446,20 +814,21 @@ template <typename real, int R>
 struct FwdPass {
   using C = cpx<real>;
   using U = Unit<real>;
+  using S = SUnit<real>;
   static constexpr int E = UnitsPerAmp<real>::E;
   static constexpr int NR = 1 << R;
   static constexpr int NU = NR >> E;
   const PassParams& P;
-  U* tile;
+  S* tile;
   C (*mats)[4];
   C* st;
   int tid;
   uint64_t gthr;
   uint32_t sthr;
   uint32_t bu;
-  C a[NR];
+  Regs<real, R> a;
 
-  __device__ __forceinline__ FwdPass(const PassParams& P_, U* tile_, C (*mats_)[4], C* psi, const real* params,
+  __device__ __forceinline__ FwdPass(const PassParams& P_, S* tile_, C (*mats_)[4], C* psi, const real* params,
                                      int n_params, const C* init, int64_t circ0)
       : P(P_), tile(tile_), mats(mats_) {
     tid = threadIdx.x;
@@ -475,7 +844,7 @@ struct FwdPass {
 #pragma unroll
     for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
 #pragma unroll
-    for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = v[k];
+    for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = to_s(v[k]);
     __syncthreads();
   }
 
@@ -485,22 +854,13 @@ struct FwdPass {
     for (int b = 0; b < ph.ntid; ++b)
       if ((tid >> b) & 1) bu ^= ph.tid_off[b];
 #pragma unroll
-    for (int j = 0; j < NU; ++j) {
-      const U v = tile[bu ^ ph.reg_off[j]];
-#pragma unroll
-      for (int k = 0; k < (1 << E); ++k) a[(j << E) + k] = v.v[k];
-    }
+    for (int j = 0; j < NU; ++j) regs_ld(a, j, tile[bu ^ ph.reg_off[j]]);
   }
 
   __device__ __forceinline__ void end(int f) {
     const Phase& ph = P.phase[f];
 #pragma unroll
-    for (int j = 0; j < NU; ++j) {
-      U v;
-#pragma unroll
-      for (int k = 0; k < (1 << E); ++k) v.v[k] = a[(j << E) + k];
-      tile[bu ^ ph.reg_off[j]] = v;
-    }
+    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
     __syncthreads();
   }
 
@@ -512,7 +872,7 @@ struct FwdPass {
   __device__ __forceinline__ void finish() {
     U* gst = reinterpret_cast<U*>(st);
 #pragma unroll
-    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = tile[sthr ^ P.sk[k]];
+    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = from_s(tile[sthr ^ P.sk[k]]);
   }
 };
 
@@ -522,12 +882,13 @@ template <typename real, int R>
 struct BwdPass {
   using C = cpx<real>;
   using U = Unit<real>;
+  using S = SUnit<real>;
   static constexpr int E = UnitsPerAmp<real>::E;
   static constexpr int NR = 1 << R;
   static constexpr int NU = NR >> E;
   const PassParams& P;
-  U* tp;
-  U* tl;
+  S* tp;
+  S* tl;
   C (*mats)[4];
   double* gacc;
   C* sp;
@@ -539,10 +900,10 @@ struct BwdPass {
   uint64_t gthr;
   uint32_t sthr;
   uint32_t bu;
-  C a[NR];
-  C l[NR];
+  Regs<real, R> a;
+  Regs<real, R> l;
 
-  __device__ __forceinline__ BwdPass(const PassParams& P_, U* smem, C (*mats_)[4], double* gacc_, C* psi, C* lam,
+  __device__ __forceinline__ BwdPass(const PassParams& P_, S* smem, C (*mats_)[4], double* gacc_, C* psi, C* lam,
                                      const real* params, int n_params_, double* grad_acc_, int64_t circ0)
       : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_) {
     tid = threadIdx.x;
@@ -566,8 +927,8 @@ struct BwdPass {
     }
 #pragma unroll
     for (int k = 0; k < NU; ++k) {
-      tp[sthr ^ P.sk[k]] = v[k];
-      tl[sthr ^ P.sk[k]] = w[k];
+      tp[sthr ^ P.sk[k]] = to_s(v[k]);
+      tl[sthr ^ P.sk[k]] = to_s(w[k]);
     }
     __syncthreads();
   }
@@ -579,13 +940,8 @@ struct BwdPass {
       if ((tid >> b) & 1) bu ^= ph.tid_off[b];
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
-      const U v = tp[bu ^ ph.reg_off[j]];
-      const U w = tl[bu ^ ph.reg_off[j]];
-#pragma unroll
-      for (int k = 0; k < (1 << E); ++k) {
-        a[(j << E) + k] = v.v[k];
-        l[(j << E) + k] = w.v[k];
-      }
+      regs_ld(a, j, tp[bu ^ ph.reg_off[j]]);
+      regs_ld(l, j, tl[bu ^ ph.reg_off[j]]);
     }
   }
 
@@ -593,14 +949,8 @@ struct BwdPass {
     const Phase& ph = P.phase[f];
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
-      U v, w;
-#pragma unroll
-      for (int k = 0; k < (1 << E); ++k) {
-        v.v[k] = a[(j << E) + k];
-        w.v[k] = l[(j << E) + k];
-      }
-      tp[bu ^ ph.reg_off[j]] = v;
-      tl[bu ^ ph.reg_off[j]] = w;
+      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
+      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
     }
     __syncthreads();
   }
@@ -661,8 +1011,8 @@ struct BwdPass {
 #pragma unroll
     for (int k = 0; k < NU; ++k) {
       const uint64_t g = (gthr | P.gk[k]) >> E;
-      reinterpret_cast<U*>(sp)[g] = tp[sthr ^ P.sk[k]];
-      reinterpret_cast<U*>(sl)[g] = tl[sthr ^ P.sk[k]];
+      reinterpret_cast<U*>(sp)[g] = from_s(tp[sthr ^ P.sk[k]]);
+      reinterpret_cast<U*>(sl)[g] = from_s(tl[sthr ^ P.sk[k]]);
     }
     if (P.n_grad) {
       __syncthreads();
@@ -685,12 +1035,12 @@ struct BwdPass {
 #define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                  \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::Unit<REAL>*>(tedq_smem_raw), tedq_mats, \
+  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  psi, params, n_params, init, circ0);
 
 #define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                  \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
   __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                                  \
-  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::Unit<REAL>*>(tedq_smem_raw), tedq_mats, \
+  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);
