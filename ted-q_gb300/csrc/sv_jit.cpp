@@ -62,20 +62,21 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
 static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
+  const int threads = 1 << (P.m - P.R);  // two CTAs per SM
   if (!adjoint) {
     snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(256, 2) tedq_fwd_%d(\n"
+             "extern \"C\" __global__ void __launch_bounds__(%d, 2) tedq_fwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
              "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long circ0) {\n"
              "  TEDQ_FWD_PROLOGUE(%s, %d)\n",
-             index, real, real, real, real, P.R);
+             threads, index, real, real, real, real, P.R);
   } else {
     snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(256, 2) tedq_bwd_%d(\n"
+             "extern \"C\" __global__ void __launch_bounds__(%d, 2) tedq_bwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
              "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long circ0) {\n"
              "  TEDQ_BWD_PROLOGUE(%s, %d)\n",
-             index, real, real, real, real, P.R);
+             threads, index, real, real, real, real, P.R);
   }
   o << buf;
   int var = 0;

@@ -540,12 +540,15 @@ cudaError_t lambda_impl(int n, const TermTable& TT, const ProbsTable& PT, const 
 
 cudaError_t launch_fwd_pass(bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
                             const void* init, int64_t batch, cudaStream_t s) {
+  // the generic kernels exist for the default register bits only
+  if (P.R != (dbl ? 4 : 5)) return cudaErrorNotSupported;
   return dbl ? fwd_impl<double, 4>(P, psi, params, n_params, init, batch, s)
              : fwd_impl<float, 5>(P, psi, params, n_params, init, batch, s);
 }
 
 cudaError_t launch_bwd_pass(bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
                             int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
+  if (P.R != (dbl ? 3 : 4)) return cudaErrorNotSupported;
   return dbl ? bwd_impl<double, 3>(P, psi, lam, params, n_params, grad_acc, batch, s)
              : bwd_impl<float, 4>(P, psi, lam, params, n_params, grad_acc, batch, s);
 }

@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iomanip>
 #include <map>
@@ -773,6 +775,22 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   gb.R = dbl ? 3 : 4;
   gf.m = std::min(mdef_f, p->ns);
   gb.m = std::min(mdef_b, p->ns);
+  // tuning override "fwd_m,fwd_R,bwd_m,bwd_R" (0 keeps a default); tile and
+  // register bits other than the defaults run on the specialised kernels only
+  if (const char* env = getenv("TEDQ_GB300_GEOMETRY")) {
+    int v[4] = {0, 0, 0, 0};
+    if (sscanf(env, "%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3]) == 4) {
+      Geometry* g2[2] = {&gf, &gb};
+      for (int i = 0; i < 2; ++i) {
+        Geometry& g = *g2[i];
+        const int m = v[2 * i] ? std::min(v[2 * i], p->ns) : g.m, R = v[2 * i + 1] ? v[2 * i + 1] : g.R;
+        if (R < 2 || R > 5 || m - R < 5 || m - R > 10 || m > kMaxTileBits)
+          throw std::invalid_argument("TEDQ_GB300_GEOMETRY out of range");
+        g.m = m;
+        g.R = R;
+      }
+    }
+  }
   gf.c = std::min(4, gf.m);
   gb.c = std::min(4, gb.m);
   p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0);
