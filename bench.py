@@ -131,17 +131,31 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """Replicas: one process per GPU from torchrun's environment; no data-path
+    collective (barriers and a max of the timings only)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
     elif torch.cuda.is_available():
         torch.cuda.set_device(0)
     return world, rank, local
+
+
+def replica_seed(base, rank):
+    """Each replica draws its own batch (weak scaling)."""
+    return base + rank
+
+
+def aggregate_rate(world, units_per_rank, ms_max):
+    """Whole-job throughput: units of all ranks over the slowest rank's time."""
+    return world * units_per_rank / (ms_max / 1000.0)
 
 
 def barrier(world):
@@ -282,7 +296,7 @@ def run_ours(a):
     info = cc.program_info
     P = cc.num_params
     B = a.batch
-    gen = torch.Generator().manual_seed(1000 + rank)
+    gen = torch.Generator().manual_seed(replica_seed(1000, rank))
     params_host = (torch.rand(a.steps + a.warmup, B, P, generator=gen) * 2 * np.pi)
     params_dev = params_host.to(dev)
     L = _lib.lib()
@@ -315,7 +329,7 @@ def run_ours(a):
     _lib.check(L.tedq_profile_read(h, prof), "tedq_profile_read")
     clk = clocks.stop()
     ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
-    value = world * B * a.steps / (ms / 1000.0)
+    value = aggregate_rate(world, B * a.steps, ms)
 
     # e2e through the public API with host buffers
     ph = params_host.pin_memory()
