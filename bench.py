@@ -64,6 +64,42 @@ def workload_config(a):
             "l2": "inputs larger than L2 (state %d MiB per circuit x batch)" % ((8 << a.qubits) >> 20)}
 
 
+def small8_spec(seed=0):
+    """8-qubit hardware-efficient ansatz: 4 layers of RY, RZ on every qubit and
+    a CNOT ring i -> i+1 mod 8; <Z_i> on every qubit (64 parameters)."""
+    rng = np.random.default_rng(seed)
+    n, gates = 8, []
+    for _ in range(4):
+        for q in range(n):
+            for name in ("RY", "RZ"):
+                gates.append({"name": name, "qubits": [q], "params": [float(rng.uniform(0, 2 * np.pi))],
+                              "trainable": [0]})
+        for q in range(n):
+            gates.append({"name": "CNOT", "qubits": [q, (q + 1) % n], "params": [], "trainable": []})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
+    return {"n": n, "gates": gates, "meas": meas, "init_state": None}
+
+
+def sv_workload(a):
+    """(spec, metric, config, loss) of the state-vector workloads."""
+    if a.workload == "small8":
+        spec = small8_spec()
+        return spec, "8q HEA value+grad circuits/s", {
+            "workload": f"hea8q_4layers_ring_batch{a.batch}", "n_qubits": 8, "layers": 4, "batch_per_gpu": a.batch,
+            "params_per_circuit": 64, "outputs": "<Z_i> i<8", "gradient": "adjoint, all parameters",
+            "l2": "states fit in L2 (2 KiB per circuit); latency-bound"}, "sum"
+    if a.workload == "mbl24":
+        from tedq_gb300.templates import mbl_spec
+        spec = mbl_spec(24, 12, seed=24)
+        P = sum(len(g["trainable"]) for g in spec["gates"])
+        return spec, "24q MBL 12-layer value+grad circuits/s", {
+            "workload": f"mbl24q_12trotter_batch{a.batch}", "n_qubits": 24, "layers": 12, "batch_per_gpu": a.batch,
+            "params_per_circuit": P, "gates": len(spec["gates"]), "outputs": "<Z_i> i<24",
+            "loss": "sum_i <Z_i>^2", "gradient": "adjoint, all parameters",
+            "l2": "inputs larger than L2 (state 128 MiB per circuit x batch)"}, "sumsq"
+    return vqc_spec(a.qubits, a.layers), METRIC, workload_config(a), "sum"
+
+
 # ---------------------------------------------------------------- helpers
 
 def read_peaks():
@@ -261,7 +297,7 @@ def plain_gpu_rate(spec, dev, n_circuits=2):
         outs = []
         Z = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex64, device=dev)
         axes = list(range(n))
-        for obs in ([[q] for q in range(n)] + [[0, 1]]):
+        for obs in [[o["qubits"][0] for o in m["obs"]] for m in spec["meas"]]:
             ms = state
             for q in obs:
                 ms = torch.tensordot(Z, ms, ([1], [q])).permute(list(range(1, q + 1)) + [0] + list(range(q + 1, n)))
@@ -287,7 +323,7 @@ def run_ours(a):
     import tedq_gb300 as qai
     from tedq_gb300 import _lib
 
-    spec = vqc_spec(a.qubits, a.layers)
+    spec, metric, config, loss_kind = sv_workload(a)
     t_compile = time.perf_counter()
     cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", fuse=not a.plain, jit=a.jit,
                                                     tile_qubits=a.tile)
@@ -303,10 +339,13 @@ def run_ours(a):
     h = cc._prog.handle
     stream = torch.cuda.current_stream(dev)
 
+    def loss_of(out):
+        return (out * out).sum() if loss_kind == "sumsq" else out.sum()
+
     def step_dev(i):
         p = params_dev[i].requires_grad_(True)
         out = cc.execute_batch(p)
-        out.sum().backward()
+        loss_of(out).backward()
         return out, p.grad
 
     for i in range(a.warmup):
@@ -336,7 +375,7 @@ def run_ours(a):
     for i in range(min(2, a.warmup)):
         p = ph[i].clone().requires_grad_(True)
         out = cc.execute_batch(p)
-        out.sum().backward()
+        loss_of(out).backward()
         out.cpu()
     torch.cuda.synchronize()
     barrier(world)
@@ -346,7 +385,7 @@ def run_ours(a):
     for i in range(a.steps):
         p = ph[a.warmup + i].detach().requires_grad_(True)   # pinned host parameters
         out = cc.execute_batch(p)                             # H2D inside
-        out.sum().backward()                                  # gradients land on the host tensor (D2H)
+        loss_of(out).backward()                               # gradients land on the host tensor (D2H)
         res = out.detach().cpu()                              # outputs D2H
         _ = p.grad.numpy()
     f1.record(stream)
@@ -379,9 +418,9 @@ def run_ours(a):
             traffic = None
     gpu_launches = prof.fwd_launches + prof.bwd_launches + prof.meas_launches + prof.lam_launches
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+    line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64", "data": "synthetic", "config": workload_config(a),
+            "dtype": "c64", "data": "synthetic", "config": config,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4,
                     "d2h_bytes_per_step": B * P * 4 + B * info["n_real_outputs"] * 4},
             "gpu_launches": int(gpu_launches),
@@ -396,18 +435,27 @@ def run_ours(a):
             "pass_kernels": "generic" if jit_reason else "specialised (NVRTC, sm_103a)",
             "compile_s": round(t_compile, 3),
             "clocks": clk}
-    if not a.no_plain:
+    if not a.no_plain and a.workload in ("vqc", "small8"):
         try:
             line["plain_gpu_per_circuit"] = {"value": plain_gpu_rate(spec, dev), "unit": UNIT,
                                              "what": "reference algorithm per circuit with torch ops on the GPU"}
             line["plain_gpu_per_circuit"]["speedup_of_value"] = value / line["plain_gpu_per_circuit"]["value"]
         except Exception as e:  # pragma: no cover
             line["plain_gpu_per_circuit"] = {"error": str(e)[:200]}
-    if not a.no_cpu:
-        spec_cpu = vqc_spec(a.qubits, a.layers)
-        k, _, _ = cpu_sample_size(spec_cpu, a.cpu_budget)
-        k = min(k, 8)
-        rate, dt = cpu_reference(spec_cpu, k)
+    if not a.no_cpu and a.workload == "mbl24":
+        # the reference's back_prop keeps every intermediate state (~380 GiB at
+        # 24 qubits): time its forward pass once
+        import oracle
+        t0 = time.perf_counter()
+        oracle.run(spec, torch.rand(P, generator=torch.Generator().manual_seed(5)) * 2 * np.pi, torch.complex64)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "circuits/s (forward only)",
+                                "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": f"1 circuit, forward only ({dt:.1f} s): back_prop does not fit host memory"}
+    elif not a.no_cpu:
+        k, _, _ = cpu_sample_size(spec, a.cpu_budget)
+        k = min(k, 8 if a.workload == "vqc" else 256)
+        rate, dt = cpu_reference(spec, k)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
                                 "sample": f"{k} circuit(s) of the workload, value+grad by back_prop, {dt:.1f} s"}
     print(json.dumps(line), flush=True)
@@ -653,7 +701,7 @@ def main():
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
-    ap.add_argument("--workload", default="vqc", choices=["vqc", "serving", "tn"])
+    ap.add_argument("--workload", default="vqc", choices=["vqc", "small8", "mbl24", "serving", "tn"])
     ap.add_argument("--tn-gemm", default="fp32", choices=["bf16x9", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--tn-graphs", type=int, default=0, help="replay each call as a CUDA graph")

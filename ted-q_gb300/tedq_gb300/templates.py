@@ -96,3 +96,34 @@ def lattice_spec(rows, cols, layers, params=None, seed=0, site=None):
         site = (rows // 2) * cols + cols // 2
     meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [int(site)]}]}]
     return {"n": n, "gates": gates, "meas": meas, "init_state": None}
+
+
+def mbl_spec(n, layers, seed, dt=0.1, J=1.0, W=5.0):
+    """1-D many-body-localisation Trotter circuit: per layer RZ(h_i dt) on every
+    site (h_i ~ U[-W, W] from ``seed``) and, on every bond, RXX(J dt) =
+    (H x H) CNOT RZ CNOT (H x H) and RZZ(J dt) = CNOT RZ CNOT, the
+    decomposition the reference's examples use; every RZ angle is trainable;
+    outputs <Z_i> on every site."""
+    rng = np.random.default_rng(seed)
+    h = rng.uniform(-W, W, n)
+    g = []
+
+    def add(name, q, p=None):
+        g.append({"name": name, "qubits": q, "params": [] if p is None else [float(p)],
+                  "trainable": [] if p is None else [0]})
+    for _ in range(layers):
+        for q in range(n):
+            add("RZ", [q], h[q] * dt)
+        for q in range(n - 1):
+            add("Hadamard", [q])
+            add("Hadamard", [q + 1])
+            add("CNOT", [q, q + 1])
+            add("RZ", [q + 1], J * dt)
+            add("CNOT", [q, q + 1])
+            add("Hadamard", [q])
+            add("Hadamard", [q + 1])
+            add("CNOT", [q, q + 1])
+            add("RZ", [q + 1], J * dt)
+            add("CNOT", [q, q + 1])
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
+    return {"n": n, "gates": g, "meas": meas, "init_state": None}

@@ -13,26 +13,9 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 qai = pytest.importorskip("tedq_gb300")
+from tedq_gb300.templates import mbl_spec  # noqa: E402
+
 DEV = "cuda:0"
-
-
-def mbl_spec(n, layers, seed, dt=0.1, J=1.0, W=5.0):
-    rng = np.random.default_rng(seed)
-    h = rng.uniform(-W, W, n)
-    g = []
-
-    def add(name, q, p=None):
-        g.append({"name": name, "qubits": q, "params": [] if p is None else [float(p)],
-                  "trainable": [] if p is None else [0]})
-    for _ in range(layers):
-        for q in range(n):
-            add("RZ", [q], h[q] * dt)
-        for q in range(n - 1):
-            add("Hadamard", [q]); add("Hadamard", [q + 1]); add("CNOT", [q, q + 1])
-            add("RZ", [q + 1], J * dt); add("CNOT", [q, q + 1]); add("Hadamard", [q]); add("Hadamard", [q + 1])
-            add("CNOT", [q, q + 1]); add("RZ", [q + 1], J * dt); add("CNOT", [q, q + 1])
-    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(n)]
-    return {"n": n, "gates": g, "meas": meas, "init_state": None}
 
 
 @pytest.mark.parametrize("n,layers", [(10, 3), (12, 2)])
