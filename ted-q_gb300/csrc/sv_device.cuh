@@ -379,6 +379,21 @@ __device__ __forceinline__ void apply_x_c(cpx<real>* a, Ctl cm) {
   }
 }
 
+// Hadamard: (x0 + x1, x0 - x1) / sqrt(2)
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_h_c(cpx<real>* a, Ctl cm) {
+  const real s = (real)0.70710678118654752440;
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) {
+    if (i & (1 << K)) continue;
+    if ((i & (unsigned)cm) != (unsigned)cm) continue;
+    const int j = i | (1 << K);
+    const cpx<real> x0 = a[i], x1 = a[j];
+    a[i] = mk<real>(s * (x0.x + x1.x), s * (x0.y + x1.y));
+    a[j] = mk<real>(s * (x0.x - x1.x), s * (x0.y - x1.y));
+  }
+}
+
 // Per-thread part of Im <lambda| G |psi> on the control subspace
 // (G = X, Y, Z or P1 = |1><1| on register bit K).
 template <int G, int K, int R, typename real, typename Ctl>
@@ -421,6 +436,10 @@ __device__ __forceinline__ void apply_ph(Regs<double, R>& A, const cpx<double>* 
 template <int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ void apply_x(Regs<double, R>& A, Ctl cm) {
   apply_x_c<K, R, double>(A.a, cm);
+}
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_h(Regs<double, R>& A, Ctl cm) {
+  apply_h_c<K, R, double>(A.a, cm);
 }
 template <int G, int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ double grad_part(const Regs<double, R>& p, const Regs<double, R>& l, Ctl cm) {
@@ -611,6 +630,34 @@ __device__ __forceinline__ void apply_x(Regs<float, R>& A, Ctl cm) {
   }
 }
 
+template <int K, int R, typename real, typename Ctl>
+__device__ __forceinline__ void apply_h(Regs<float, R>& A, Ctl cm) {
+  TEDQ_GROUPS
+  const float s = 0.70710678118654752440f;
+  if constexpr (K == 0) {
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if ((g & cg) != cg) continue;
+      const float2 xr = A.re[g], xi = A.im[g];
+      A.re[g] = make_float2(s * (xr.x + xr.y), s * (xr.x - xr.y));
+      A.im[g] = make_float2(s * (xi.x + xi.y), s * (xi.x - xi.y));
+    }
+  } else {
+    const float2 S = bc2(s), NS = bc2(-s);
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      if (g & (1 << (K - 1))) continue;
+      if ((g & cg) != cg) continue;
+      const int h = g | (1 << (K - 1));
+      const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+      A.re[g] = odd_only(c0, xr0, fma2(S, xr0, mul2(S, xr1)));
+      A.im[g] = odd_only(c0, xi0, fma2(S, xi0, mul2(S, xi1)));
+      A.re[h] = odd_only(c0, xr1, fma2(S, xr0, mul2(NS, xr1)));
+      A.im[h] = odd_only(c0, xi1, fma2(S, xi0, mul2(NS, xi1)));
+    }
+  }
+}
+
 template <int G, int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ float grad_part(const Regs<float, R>& p, const Regs<float, R>& l, Ctl cm) {
   TEDQ_GROUPS
@@ -678,6 +725,7 @@ __device__ __forceinline__ void dispatch_gate(int kind, int k, Regs<real, R>& a,
         case GK_RXT: apply_rxt<K, R, real>(a, M, cm); break;
         case GK_RYT: apply_ryt<K, R, real>(a, M, cm); break;
         case GK_PH: apply_ph<K, R, real>(a, M, cm); break;
+        case GK_H: apply_h<K, R, real>(a, cm); break;
         default: apply_x<K, R, real>(a, cm); break;
       }
     } else {

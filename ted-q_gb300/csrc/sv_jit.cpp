@@ -47,6 +47,10 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
       snprintf(buf, sizeof buf, "  apply_x<%d, %d, %s>(%s, CM<%s>{});\n", r.k0, R, real, arr, cm(r.cmask).c_str());
       o << buf;
       break;
+    case GK_H:
+      snprintf(buf, sizeof buf, "  apply_h<%d, %d, %s>(%s, CM<%s>{});\n", r.k0, R, real, arr, cm(r.cmask).c_str());
+      o << buf;
+      break;
     default: {  // GK_SWAP as three controlled bit flips
       const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
       const int tg[3] = {r.k1, r.k0, r.k1};

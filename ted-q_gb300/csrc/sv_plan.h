@@ -48,6 +48,7 @@ enum GateKind : uint8_t {
   GK_RXT = 4,   // [[c, -i s], [-i s, c]]: c = M[0].re, s = -M[1].im (4 FMA/amplitude)
   GK_RYT = 5,   // [[c, -s], [s, c]]:      c = M[0].re, s = -M[1].re
   GK_PH = 6,    // diag(1, d): only the |1> half is multiplied (d = matrix entry 1)
+  GK_H = 7,     // Hadamard (x0 + x1, x0 - x1) / sqrt(2) (no matrix)
 };
 
 // Generator kinds of the adjoint gradient: the gradient of a gate

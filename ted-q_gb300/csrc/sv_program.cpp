@@ -359,9 +359,18 @@ static uint64_t fill_bits(uint64_t mask, int want, int limit) {
   return mask;
 }
 
+// A lone Hadamard factor (runs its own matrix-free register code).
+static bool is_hadamard(const HGate& g) {
+  if (g.kind != GK_U1 || g.factors.size() != 1 || g.factors[0].op != F_FIXED2) return false;
+  const CD* m = g.factors[0].m;
+  return m[0].re == kInvSqrt2 && m[1].re == kInvSqrt2 && m[2].re == kInvSqrt2 && m[3].re == -kInvSqrt2 &&
+         m[0].im == 0.0 && m[1].im == 0.0 && m[2].im == 0.0 && m[3].im == 0.0;
+}
+
 // Register kind of a gate: structured one-factor rotations and phase-type
 // diagonals get cheaper register code than a dense / general diagonal matrix.
 static uint8_t specialised_kind(const HGate& g) {
+  if (is_hadamard(g)) return GK_H;
   if (g.kind == GK_U1 && g.factors.size() == 1) {
     if (g.factors[0].op == F_RX) return GK_RXT;
     if (g.factors[0].op == F_RY) return GK_RYT;
@@ -379,6 +388,7 @@ static uint8_t specialised_kind(const HGate& g) {
 struct Cap {
   int gates = 0, mats = 0, factors = 0, fixed = 0, grads = 0;
   bool fits(const HGate& g) const {
+    if (is_hadamard(g)) return gates + 1 <= kMaxPassGates;
     int nf = (int)g.factors.size(), nfix = 0;
     for (auto& f : g.factors) nfix += (f.op == F_FIXED2) ? 4 : (f.op == F_FIXD ? 2 : 0);
     if (g.kind == kDense) nfix = (int)g.dmat.size();
@@ -388,6 +398,7 @@ struct Cap {
   }
   void add(const HGate& g) {
     gates += 1;
+    if (is_hadamard(g)) return;
     if (g.kind == GK_U1 || g.kind == GK_D1) mats += 1;
     factors += (int)g.factors.size();
     for (auto& f : g.factors) fixed += (f.op == F_FIXED2) ? 4 : (f.op == F_FIXD ? 2 : 0);
@@ -543,7 +554,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
         r.coef = g.coef;
         P.n_grad++;
       }
-      if (g.kind == GK_U1 || g.kind == GK_D1) {  // (also RXT / RYT / PH)
+      if ((g.kind == GK_U1 || g.kind == GK_D1) && r.kind != GK_H) {  // (also RXT / RYT / PH)
         MatDesc& md = P.mat[P.n_mats];
         r.mat = (uint8_t)P.n_mats++;
         md.diag = g.kind == GK_D1;

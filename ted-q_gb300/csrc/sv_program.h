@@ -35,7 +35,7 @@ struct HGate {
   float coef = 0.f;
   uint64_t bits() const;
 };
-constexpr uint8_t kDense = 7;
+constexpr uint8_t kDense = 15;
 
 struct Term {            // Hermitian Pauli string (-i)^ny X^x Z^z
   uint64_t x = 0, z = 0;

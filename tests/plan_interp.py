@@ -12,7 +12,7 @@ lowering and the Pauli expansion of the observables without a GPU.
 import numpy as np
 
 F_FIXED2, F_FIXD, F_RX, F_RY, F_RZ, F_PHASE, F_ROT = range(7)
-GK_U1, GK_D1, GK_X, GK_SWAP, GK_RXT, GK_RYT, GK_PH = range(7)
+GK_U1, GK_D1, GK_X, GK_SWAP, GK_RXT, GK_RYT, GK_PH, GK_H = range(8)
 GR_NONE, GR_X, GR_Y, GR_Z, GR_P1 = range(5)
 
 
@@ -78,6 +78,9 @@ def _apply(a, r, M):
     elif kind == GK_PH:
         M = np.diag([1.0, M[1, 1]])
         kind = GK_D1
+    elif kind == GK_H:
+        M = np.array([[1.0, 1.0], [1.0, -1.0]], dtype=complex) / np.sqrt(2.0)
+        kind = GK_U1
     for i in range(NR):
         if kind == GK_D1:
             if (i & cm) == cm:
@@ -183,7 +186,7 @@ def run_pass(P, psi, prm, lam=None, grads=None):
             a = tp[addr]
             l = tl[addr] if tl is not None else None
             for r in ph["gates"]:
-                M = mats[r["mat"]] if r["kind"] not in (GK_X, GK_SWAP) else None
+                M = mats[r["mat"]] if r["kind"] not in (GK_X, GK_SWAP, GK_H) else None
                 if l is not None and r["grad"] != GR_NONE:
                     grads[r["slot"]] += _grad(a, l, r)
                 _apply(a, r, M)
