@@ -79,6 +79,25 @@ class Circuit:
     def init_state(self):
         return self._init_state
 
+    # ------------------------------------------------ quantum natural gradient
+    def cycabc(self, numarg):
+        """Layering for the metric tensor (circuit.py:101-164)."""
+        from .qng import layer_blocks
+        return layer_blocks(self, numarg)
+
+    def gen_circuits(self, numarg, **kwargs):
+        """Per-layer circuits of the metric tensor (circuit.py:166-203), compiled
+        for the GB300 backend; returns the ``MetricTensor`` that
+        ``metric_tensor`` evaluates (the reference returns a list of circuits
+        compiled again on every call)."""
+        from .qng import MetricTensor
+        return MetricTensor(self, numarg, **kwargs)
+
+    def metric_tensor(self, circuits_list, *parameters):
+        """Block-diagonal metric tensor (circuit.py:297-316) for the circuit's
+        flat parameters."""
+        return circuits_list(*parameters)
+
     def compilecircuit(self, backend=None, **kwargs):
         """Compile for ``backend``; ``"gb300"`` is the GB300 backend."""
         if backend == "gb300":
