@@ -14,7 +14,7 @@ from .measurement import (Expectation, MeasurementReturnTypes, Probability, Quan
 from .operators import (CNOT, CRX, CRY, CRZ, CSWAP, CY, CZ, RX, RY, RZ, SWAP, SX, ControlledPhaseShift,  # noqa: F401
                         GateBase, Hadamard, I, IintStateVector, ObservableBase, OperatorBase, PauliX, PauliY,
                         PauliZ, PhaseShift, Rot, S, T, Toffoli, Unitary)
-from .backend import GB300Backend, GB300Execute, GB300ParamShift, GB300TnExecute  # noqa: F401
+from .backend import GB300QUDIO, GB300Backend, GB300Execute, GB300ParamShift, GB300TnExecute  # noqa: F401
 from .circuit_io import FromQasmFile  # noqa: F401
 from .qng import QNG, MetricTensor  # noqa: F401
 from .reference_bridge import register_with_tedq  # noqa: F401

@@ -743,3 +743,44 @@ class _PsiShape:
 
     def __getitem__(self, item):
         raise RuntimeError("state output requested from a program without state measurement")
+
+
+class GB300QUDIO(GB300Backend):
+    """Dataset-parallel evaluation: replaces ``QUDIOBackend``
+    (tedq/backends/qudio_backend.py:45-124), which wraps the pytorch backend in
+    ``torch.nn.DataParallel`` and evaluates one dataset row per GPU per step.
+    Here every row of the dataset becomes one circuit of a single native batch:
+    row ``i`` binds ``(x_i, *params)`` positionally (data first, as the
+    reference's ``TorchModel.forward`` passes them), and the results are
+    concatenated along dim 0 like the reference's loop.  Gradients reach
+    ``params`` through the batched adjoint backward."""
+
+    def __init__(self, backend, circuit, **kwargs):
+        super().__init__(backend, circuit, **kwargs)
+        self._dataset = None
+
+    def set_dataset(self, dataset):
+        self._dataset = torch.as_tensor(dataset)
+
+    @property
+    def dataset(self):
+        return self._dataset
+
+    @property
+    def device(self):
+        return "cuda:0" if torch.cuda.is_available() else "cpu"
+
+    def __call__(self, *params):
+        if self._dataset is None:
+            raise ValueError("no dataset: call set_dataset first")
+        X = self._dataset
+        n = X.shape[0]
+        theta = self._flatten(params) if params else torch.zeros(0)
+        dev = self._cuda_device(theta.device if isinstance(theta, torch.Tensor) else None)
+        dtype = torch.float64 if self._precision == "c128" else torch.float32
+        P = torch.cat([X.reshape(n, -1).to(dev, dtype), theta.reshape(1, -1).to(dev, dtype).expand(n, -1)], 1)
+        if P.shape[1] != self._prog.n_params:
+            raise ValueError(f"Error!!!! number of parameters are not matched!! required {self._prog.n_params} "
+                             f"but {P.shape[1]} are given (dataset row + params)")
+        out = self.execute_batch(P)
+        return out.reshape((-1,) + tuple(out.shape[2:]))

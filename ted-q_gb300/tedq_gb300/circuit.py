@@ -103,6 +103,9 @@ class Circuit:
         if backend == "gb300":
             from .backend import GB300Backend
             return GB300Backend(backend, self, **kwargs)
+        if backend == "gb300_QUDIO":
+            from .backend import GB300QUDIO
+            return GB300QUDIO(backend, self, **kwargs)
         raise ValueError(f"{backend}: unknown backend input")
 
     def __str__(self):
