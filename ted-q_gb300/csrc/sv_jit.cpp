@@ -66,21 +66,24 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
 static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
-  const int threads = 1 << (P.m - P.R);  // two CTAs per SM
+  // two CTAs per SM when their shared memory fits (tile + matrices + gradient slots)
+  const int threads = 1 << (P.m - P.R);
+  const int tile_bytes = (adjoint ? 32 : 16) << (P.m - P.e), static_bytes = adjoint ? 15 * 1024 : 5 * 1024;
+  const int min_blocks = 2 * (tile_bytes + static_bytes) <= 227 * 1024 ? 2 : 1;
   if (!adjoint) {
     snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(%d, 2) tedq_fwd_%d(\n"
+             "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
              "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long circ0) {\n"
              "  TEDQ_FWD_PROLOGUE(%s, %d)\n",
-             threads, index, real, real, real, real, P.R);
+             threads, min_blocks, index, real, real, real, real, P.R);
   } else {
     snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(%d, 2) tedq_bwd_%d(\n"
+             "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_bwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
              "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long circ0) {\n"
              "  TEDQ_BWD_PROLOGUE(%s, %d)\n",
-             threads, index, real, real, real, real, P.R);
+             threads, min_blocks, index, real, real, real, real, P.R);
   }
   o << buf;
   int var = 0;
@@ -389,7 +392,7 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
       err = "missing kernel " + srcs[i].name;
       return false;
     }
-    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 64 * 1024);
+    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 200 * 1024);
     ((int)i < n_fwd ? out.fwd : out.bwd).push_back(reinterpret_cast<void*>(f));
   }
   return true;
