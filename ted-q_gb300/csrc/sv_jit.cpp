@@ -66,10 +66,12 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
 static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
-  // two CTAs per SM when their shared memory fits (tile + matrices + gradient slots)
+  // as many CTAs per SM as their shared memory (tile + matrices + gradient
+  // slots) allows while every thread may keep 128 registers
   const int threads = 1 << (P.m - P.R);
   const int tile_bytes = (adjoint ? 32 : 16) << (P.m - P.e), static_bytes = adjoint ? 15 * 1024 : 5 * 1024;
-  const int min_blocks = 2 * (tile_bytes + static_bytes) <= 227 * 1024 ? 2 : 1;
+  int min_blocks = std::min((227 * 1024) / (tile_bytes + static_bytes), 65536 / (threads * 128));
+  min_blocks = std::max(1, std::min(min_blocks, 8));
   if (!adjoint) {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
