@@ -15,6 +15,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -191,8 +192,7 @@ int32_t ensure_device(tedq_tn_plan* p, int dev) {
     cublasStatus_t st = B.create(&D.handle);
     if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasCreate", st);
     if (p->precision == TEDQ_PREC_C64 && (p->gemm == TEDQ_TN_GEMM_BF16X9 || p->gemm == TEDQ_TN_GEMM_AUTO)) {
-      st = B.set_emulation(D.handle, p->gemm == TEDQ_TN_GEMM_AUTO ? CUBLAS_EMULATION_STRATEGY_PERFORMANT
-                                                                  : CUBLAS_EMULATION_STRATEGY_EAGER);
+      st = B.set_emulation(D.handle, CUBLAS_EMULATION_STRATEGY_EAGER);
       if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetEmulationStrategy", st);
     }
   }
@@ -257,8 +257,12 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
   cublasComputeType_t ct = CUBLAS_COMPUTE_64F;
   if (!dbl)
     ct = p->gemm == TEDQ_TN_GEMM_TF32   ? CUBLAS_COMPUTE_32F_FAST_TF32
-         : p->gemm == TEDQ_TN_GEMM_FP32 ? CUBLAS_COMPUTE_32F
-                                        : CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+         : p->gemm == TEDQ_TN_GEMM_BF16X9 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
+                                          : CUBLAS_COMPUTE_32F;
+  // AUTO: BF16x9 on the tensor cores for contractions of at least 2^auto_log2
+  // real flops per circuit, FP32 below
+  int auto_log2 = 24;
+  if (const char* env = getenv("TEDQ_GB300_TN_AUTO_LOG2")) auto_log2 = atoi(env);
   const real one = 1, zero = 0;
   const int n_meas = (int)p->nets.size();
   for (int m = 0; m < n_meas; ++m) {
@@ -329,10 +333,14 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         // [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B] (A doubled); K is doubled either way
         const long long mr = stp.double_a ? 2 * M : M, nr = stp.double_a ? N : 2 * N;
         const long long sa = A.op[0].nb > 1 ? mr * 2 * K : 0, sb = A.op[1].nb > 1 ? nr * 2 * K : 0;
+        const cublasComputeType_t cts =
+            (!dbl && p->gemm == TEDQ_TN_GEMM_AUTO && 8.0 * M * N * K >= std::ldexp(1.0, auto_log2))
+                ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
+                : ct;
         rc = timed(p, s, 2, 8.0 * M * N * K * nbatch, [&]() -> int32_t {
           st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)mr, (int)nr, (int)(2 * K), &one, A.op[0].dst, dt,
                        (int)(2 * K), sa, A.op[1].dst, dt, (int)(2 * K), sb, &zero, C, dt, (int)mr, 2 * M * N, nbatch,
-                       ct, CUBLAS_GEMM_DEFAULT);
+                       cts, CUBLAS_GEMM_DEFAULT);
           if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
           return TEDQ_OK;
         });
