@@ -294,9 +294,54 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         o.src_bstride = T.batched ? (2ll << (T.lm + T.ln)) : 0;
       }
     };
+    // fused operand: per-bit offsets (reals) of the source storage
+    auto fused_op = [&](const TnOperand& op, int64_t sl, TnFusedOp& o) {
+      const TnTensor& T = net.tensors[op.tensor];
+      const int64_t M = 1ll << T.lm, N = 1ll << T.ln;
+      const int64_t sj = T.split ? 2 * M : M;
+      auto w = [&](int sbit) -> int64_t {
+        if (T.leaf >= 0) return 2ll << sbit;
+        return sbit < T.lm ? (1ll << sbit) : (sj << (sbit - T.lm));
+      };
+      std::memset(&o, 0, sizeof(o));
+      if (T.leaf >= 0) {
+        o.src = T.batched ? leaves + 2 * T.off * batch : consts + 2 * T.off;
+        o.bstride = T.batched ? (2ll << T.full_idx.size()) : 0;
+        o.im = 1;
+        for (auto& qb : op.slice_bit) o.base += ((sl >> qb.first) & 1) ? w(qb.second) : 0;
+      } else {
+        o.src = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
+        o.bstride = T.batched ? (2ll << (T.lm + T.ln)) : 0;
+        o.im = T.split ? M : M * N;
+      }
+      for (int j = 0; j < op.nc; ++j) o.wk[j] = w(op.src_bit[j]);
+      for (int j = 0; j < op.nf; ++j) o.wf[j] = w(op.src_bit[op.nc + j]);
+    };
     const int64_t n_slices = 1ll << net.sliced.size();
     for (int64_t sl = 0; sl < n_slices; ++sl) {
       for (const TnStep& stp : net.steps) {
+        if (stp.fused) {
+          const TnTensor& T = net.tensors[stp.out];
+          TnFusedArgs F;
+          std::memset(&F, 0, sizeof(F));
+          fused_op(stp.opa, sl, F.a);
+          fused_op(stp.opb, sl, F.b);
+          F.lm = stp.opa.nf;
+          F.ln = stp.opb.nf;
+          F.lk = stp.opa.nc;
+          if (F.lm > kTnMaxBits || F.ln > kTnMaxBits)
+            return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: fused operand above 2^48 entries");
+          F.nb = stp.batched ? batch : 1;
+          F.dst = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
+          F.dst_bstride = T.batched ? (2ll << (T.lm + T.ln)) : 0;
+          const double flops = 8.0 * std::ldexp(1.0, F.lm + F.ln + F.lk) * (double)F.nb;
+          int32_t rc = timed(p, s, 2, flops, [&]() -> int32_t {
+            TEDQ_CUDA("tedq_tn_contract: fused kernel", tn_fused<real>(F, s));
+            return TEDQ_OK;
+          });
+          if (rc != TEDQ_OK) return rc;
+          continue;
+        }
         TnGatherArgs A;
         std::memset(&A, 0, sizeof(A));
         const TnOperand* ops[2] = {&stp.opa, &stp.opb};

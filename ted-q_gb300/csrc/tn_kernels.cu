@@ -1,15 +1,15 @@
 // tn_kernels.cu -- kernels of the tensor-network mode (tn_kernels.cuh).
 //
 // Work per pairwise contraction of A (M x K) and B (K x N), complex:
-//  * one gather launch writes both planar real operands [Re A; Im A] (2M x K,
-//    K contiguous) and [Re B, Im B] (K contiguous per column): a bit
-//    permutation of the source index, fused with the complex combination of
-//    the producer's real product when the source is an intermediate;
-//  * one real GEMM (2M x 2N x K) on the tensor cores (cuBLAS), whose four
-//    blocks are ArBr, ArBi, AiBr, AiBi -- the 4M real decomposition; the
-//    complex result is formed by whichever gather reads it next.
-// Gather traffic per operand entry: 8 B read from a leaf or 16 B from a real
-// product (c64), 8 B written.
+//  * small contractions (the planner's `fused` steps): one tn_fused_kernel
+//    launch reads both operands in place through additive per-bit offsets and
+//    writes the planar complex result;
+//  * large ones: one gather launch writes both operands as rows of the real
+//    embedding ([Re, Im], and [Re, -Im] / [Im, Re] for the doubled operand),
+//    then one real GEMM over the batch (cuBLAS; BF16x9 tensor-core emulation
+//    or FP32) produces [Re C, Im C] -- the 4M decomposition in one product.
+// Gather traffic per operand entry (c64): 8 B read, 8 B written (16 B for the
+// doubled operand).
 #include <cuda_runtime.h>
 
 #include "launch.cuh"
@@ -131,6 +131,51 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   }
 }
 
+// One thread per (circuit, output element); the contracted-index offsets of
+// both operands are tabulated once per CTA in shared memory.
+template <typename real>
+__global__ void __launch_bounds__(256) tn_fused_kernel(const __grid_constant__ TnFusedArgs A) {
+  __shared__ int64_t koff[2][256];
+  const int K = 1 << A.lk;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    int64_t oa = 0, ob = 0;
+    for (int j = 0; j < A.lk; ++j)
+      if ((k >> j) & 1) {
+        oa += A.a.wk[j];
+        ob += A.b.wk[j];
+      }
+    koff[0][k] = oa;
+    koff[1][k] = ob;
+  }
+  __syncthreads();
+  const int lmn = A.lm + A.ln;
+  const int64_t MN = 1ll << lmn, total = MN * A.nb, imask = (1ll << A.lm) - 1;
+  const real* sa = static_cast<const real*>(A.a.src);
+  const real* sb = static_cast<const real*>(A.b.src);
+  real* dst = static_cast<real*>(A.dst);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t >> lmn, idx = t & (MN - 1);
+    const int64_t i = idx & imask, j = idx >> A.lm;
+    int64_t oa = A.a.base + b * A.a.bstride, ob = A.b.base + b * A.b.bstride;
+    for (int q = 0; q < A.lm; ++q)
+      if ((i >> q) & 1) oa += A.a.wf[q];
+    for (int q = 0; q < A.ln; ++q)
+      if ((j >> q) & 1) ob += A.b.wf[q];
+    const real* pa = sa + oa;
+    const real* pb = sb + ob;
+    real re = 0, im = 0;
+    for (int k = 0; k < K; ++k) {
+      const real ar = pa[koff[0][k]], ai = pa[koff[0][k] + A.a.im];
+      const real br = pb[koff[1][k]], bi = pb[koff[1][k] + A.b.im];
+      re = fma(ar, br, fma(-ai, bi, re));
+      im = fma(ar, bi, fma(ai, br, im));
+    }
+    real* d = dst + b * A.dst_bstride;
+    d[idx] = re;
+    d[MN + idx] = im;
+  }
+}
+
 template <typename real>
 __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
                                real* out, int n_meas, int m, int first, int last) {
@@ -169,6 +214,15 @@ cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
 }
 
 template <typename real>
+cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream) {
+  if (args.lk > 8) return cudaErrorInvalidValue;
+  const int64_t total = (1ll << (args.lm + args.ln)) * args.nb;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  return launch_kernel(tn_fused_kernel<real>, dim3((unsigned)blocks), dim3(256), 0, stream, args);
+}
+
+template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
                     int m, int first, int last, cudaStream_t stream) {
   const unsigned blocks = (unsigned)((batch + 255) / 256);
@@ -181,6 +235,8 @@ template cudaError_t tn_build_leaves<double>(const TnLeafDesc*, int, const doubl
                                              cudaStream_t);
 template cudaError_t tn_gather<float>(const TnGatherArgs&, cudaStream_t);
 template cudaError_t tn_gather<double>(const TnGatherArgs&, cudaStream_t);
+template cudaError_t tn_fused<float>(const TnFusedArgs&, cudaStream_t);
+template cudaError_t tn_fused<double>(const TnFusedArgs&, cudaStream_t);
 template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int, cudaStream_t);
 template cudaError_t tn_root<double>(const double*, int64_t, int64_t, double*, double*, int, int, int, int,
                                      cudaStream_t);

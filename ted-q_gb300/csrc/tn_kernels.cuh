@@ -46,6 +46,32 @@ struct TnGatherArgs {
   TnGatherOp op[2];
 };
 
+// One operand of a fused contraction, read in place: element (f, k) of the
+// operand's [F][K] view has its real part at src + b * bstride + base +
+// sum_j bit_j(f) * wf[j] + sum_j bit_j(k) * wk[j] (reals) and its imaginary
+// part `im` reals further.
+struct TnFusedOp {
+  const void* src;
+  int64_t bstride;
+  int64_t base;
+  int64_t im;
+  int64_t wf[kTnMaxBits];
+  int64_t wk[kTnMaxBits];
+};
+
+// C[b](i, j) = sum_k A[b](i, k) B[b](k, j), written planar: Re at j * M + i,
+// Im at + M * N (M = 2^lm, N = 2^ln, K = 2^lk <= 256).
+struct TnFusedArgs {
+  TnFusedOp a, b;
+  void* dst;
+  int64_t dst_bstride;
+  int64_t nb;  // batch entries
+  int32_t lm, ln, lk, pad;
+};
+
+template <typename real>
+cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream);
+
 template <typename real>
 cudaError_t tn_build_leaves(const TnLeafDesc* desc, int n_desc, const real* params, int n_params, int64_t batch,
                             real* leaves, cudaStream_t stream);

@@ -556,6 +556,12 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
     };
     st.opa = operand(st.a, st.free_a);
     st.opb = operand(st.b, st.free_b);
+    {
+      const int lm = (int)st.free_a.size(), ln = (int)st.free_b.size(), lk = (int)st.contracted.size();
+      // small contractions with enough outputs (or a short sum) per circuit
+      st.fused = lm + ln + lk < opt.fused_log2 && lk <= 8 && (lm + ln >= 5 || lk <= 6);
+      if (st.fused) st.double_a = false;
+    }
     for (int t : {st.a, st.b}) {
       const TnTensor& T = net.tensors[t];
       if (T.leaf >= 0) continue;
@@ -584,6 +590,7 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
 int64_t tn_scratch_reals(const TnNet& net, int64_t batch) {
   int64_t m = 0;
   for (const TnStep& s : net.steps) {
+    if (s.fused) continue;
     int64_t ba = net.tensors[s.a].batched ? batch : 1, bb = net.tensors[s.b].batched ? batch : 1;
     int64_t v = ((s.opa.doubled ? 4ll : 2ll) << (s.opa.nf + s.opa.nc)) * ba +
                 ((s.opb.doubled ? 4ll : 2ll) << (s.opb.nf + s.opb.nc)) * bb;
@@ -649,7 +656,8 @@ std::string tn_describe(const std::vector<TnNet>& nets, int n_params, int precis
     for (size_t i = 0; i < n.steps.size(); ++i) {
       const TnStep& s = n.steps[i];
       o << (i ? "," : "") << "{\"a\":" << s.a << ",\"b\":" << s.b << ",\"out\":" << s.out
-        << ",\"batched\":" << (s.batched ? 1 : 0) << ",\"double_a\":" << (s.double_a ? 1 : 0) << ",\"opa\":";
+        << ",\"batched\":" << (s.batched ? 1 : 0) << ",\"double_a\":" << (s.double_a ? 1 : 0)
+        << ",\"fused\":" << (s.fused ? 1 : 0) << ",\"opa\":";
       operand_json(o, s.opa);
       o << ",\"opb\":";
       operand_json(o, s.opb);

@@ -84,6 +84,9 @@ struct TnStep {
   TnOperand opa, opb;
   bool batched = false;
   bool double_a = false;  // A is the doubled operand (result in "split" layout)
+  // small contraction: one fused kernel reads both operands in place and
+  // writes the planar result (no gathers, no GEMM call)
+  bool fused = false;
 };
 
 struct TnNet {
@@ -108,6 +111,7 @@ struct TnNet {
 };
 
 struct TnPlanOptions {
+  int fused_log2 = 20;  // contractions below 2^fused_log2 complex MACs per circuit run fused
   int max_rank = 27;   // slice until every intermediate has at most 2^max_rank entries
   int repeats = 64;    // randomised greedy trials (the first is plain greedy)
   uint64_t seed = 1;

@@ -37,6 +37,28 @@ def _leaf(net, t, prm):
     return c[0::2] + 1j * c[1::2]
 
 
+def _complex(net, op, store, sl):
+    """Operand values as a complex [F, K] array (rows: free index, columns:
+    contracted index), read through the step's bit map."""
+    T = net["tensors"][op["tensor"]]
+    nbits = op["nf"] + op["nc"]
+    e = np.arange(1 << nbits, dtype=np.int64)
+    flat = np.zeros_like(e)
+    for q, bit in op["slice_bit"]:
+        flat += ((sl >> q) & 1) << bit
+    for j, bit in enumerate(op["src_bit"]):
+        flat += ((e >> j) & 1) << bit
+    src = store[op["tensor"]]
+    if T["leaf"] >= 0:
+        vals = src[flat]
+    else:
+        M, N = 1 << T["lm"], 1 << T["ln"]
+        i, j = flat & (M - 1), flat >> T["lm"]
+        sj, sp = (2 * M, M) if T["split"] else (M, M * N)
+        vals = src[j * sj + i] + 1j * src[j * sj + i + sp]
+    return vals.reshape(1 << op["nf"], 1 << op["nc"])
+
+
 def _gather(net, op, store, sl):
     T = net["tensors"][op["tensor"]]
     nbits = op["nf"] + op["nc"]
@@ -69,6 +91,11 @@ def run_net(net, prm):
     for sl in range(1 << len(net["sliced"])):
         store = dict(leaves)
         for st in net["steps"]:
+            if st["fused"]:
+                # fused kernel: complex product written planar (Re at j*M + i, Im at + M*N)
+                C = _complex(net, st["opa"], store, sl) @ _complex(net, st["opb"], store, sl).T
+                store[st["out"]] = np.concatenate([C.real.T.reshape(-1), C.imag.T.reshape(-1)])
+                continue
             A = _gather(net, st["opa"], store, sl)  # rows of op(A)
             B = _gather(net, st["opb"], store, sl)  # columns of B
             store[st["out"]] = (A @ B.T).reshape(-1, order="F")  # column-major result
