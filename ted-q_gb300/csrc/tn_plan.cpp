@@ -562,11 +562,17 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
       st.fused = lm + ln + lk < opt.fused_log2 && lk <= 8 && (lm + ln >= 5 || lk <= 6);
       if (st.fused) st.double_a = false;
     }
-    for (int t : {st.a, st.b}) {
-      const TnTensor& T = net.tensors[t];
-      if (T.leaf >= 0) continue;
-      (T.batched ? ab : au).release(T.arena, inter_reals(T));
-    }
+    // a gathered step copies its inputs to the operand scratch before the
+    // GEMM writes, so its output may reuse their space; a fused step reads
+    // its inputs while it writes, so its output is placed first
+    auto release_inputs = [&]() {
+      for (int t : {st.a, st.b}) {
+        const TnTensor& T = net.tensors[t];
+        if (T.leaf >= 0) continue;
+        (T.batched ? ab : au).release(T.arena, inter_reals(T));
+      }
+    };
+    if (!st.fused) release_inputs();
     TnTensor out;
     out.idx = st.free_b;
     out.idx.insert(out.idx.end(), st.free_a.begin(), st.free_a.end());
@@ -575,6 +581,7 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
     out.split = st.double_a;
     out.batched = st.batched;
     out.arena = (out.batched ? ab : au).alloc(inter_reals(out));
+    if (st.fused) release_inputs();
     st.out = (int)net.tensors.size();
     net.tensors.push_back(out);
     net.steps.push_back(std::move(st));

@@ -109,14 +109,16 @@ def run(desc, prm):
 
 def check_arenas(net):
     """Live intermediates never overlap in their arena (batched and unbatched
-    separately); the output of a step may reuse the space of its inputs."""
+    separately); the output of a gathered step may reuse the space of its
+    inputs, the output of a fused step (which reads its inputs in place) not."""
     T = net["tensors"]
     L = net["n_leaves"]
     live = {}
     for st in net["steps"]:
-        for t in (st["a"], st["b"]):
-            if t >= L:
-                live.pop(t)
+        if not st["fused"]:
+            for t in (st["a"], st["b"]):
+                if t >= L:
+                    live.pop(t)
         o = st["out"]
         size = 2 << (T[o]["lm"] + T[o]["ln"])
         lo, hi = T[o]["arena"], T[o]["arena"] + size
@@ -125,5 +127,9 @@ def check_arenas(net):
         for t, (b, l2, h2) in live.items():
             if b == T[o]["batched"]:
                 assert hi <= l2 or h2 <= lo, f"tensor {o} overlaps live tensor {t}"
+        if st["fused"]:
+            for t in (st["a"], st["b"]):
+                if t >= L:
+                    live.pop(t)
         live[o] = (T[o]["batched"], lo, hi)
     assert list(live) == [net["root"]]
