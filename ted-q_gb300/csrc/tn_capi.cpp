@@ -486,6 +486,7 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
       if (opts->repeats > 0) po.repeats = opts->repeats;
       if (opts->seed) po.seed = opts->seed;
     }
+    if (const char* env = getenv("TEDQ_GB300_TN_FUSED_LOG2")) po.fused_log2 = atoi(env);  // tuning
     p->n = n_qubits;
     for (int i = 0; i < n_gates && gates; ++i)
       for (int j = 0; j < 3; ++j) p->n_params = std::max(p->n_params, gates[i].param_slot[j] + 1);
