@@ -111,7 +111,7 @@ struct TnNet {
 };
 
 struct TnPlanOptions {
-  int fused_log2 = 20;  // contractions below 2^fused_log2 complex MACs per circuit run fused
+  int fused_log2 = 13;  // contractions below 2^fused_log2 complex MACs per circuit run fused
   int max_rank = 27;   // slice until every intermediate has at most 2^max_rank entries
   int repeats = 64;    // randomised greedy trials (the first is plain greedy)
   uint64_t seed = 1;
