@@ -702,7 +702,7 @@ def main():
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
     ap.add_argument("--workload", default="vqc", choices=["vqc", "small8", "mbl24", "serving", "tn"])
-    ap.add_argument("--tn-gemm", default="fp32", choices=["bf16x9", "tf32", "fp32", "auto"])
+    ap.add_argument("--tn-gemm", default="auto", choices=["bf16x9", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--tn-graphs", type=int, default=0, help="replay each call as a CUDA graph")
     ap.add_argument("--rates", default="100,500,2000,5000")

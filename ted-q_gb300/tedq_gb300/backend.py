@@ -215,7 +215,7 @@ class NativeTnPlan:
     per expectation value, planned once, contracted for a whole parameter
     batch per call as gathers + real GEMMs on the tensor cores."""
 
-    def __init__(self, circuit, precision="c64", gemm="fp32", max_rank=0, repeats=0, seed=0, graphs=False):
+    def __init__(self, circuit, precision="c64", gemm="auto", max_rank=0, repeats=0, seed=0, graphs=False):
         L = _lib.lib()
         if circuit.init_state is not None:
             raise NotImplementedError("the tensor-network mode starts from |0...0>")
@@ -434,7 +434,7 @@ class GB300Backend:
         # path optimisers, so their objects and hyper_opt are not called
         self._tn = bool(tn_mode or use_jdopttn or use_cotengra)
         if self._tn:
-            self._prog = NativeTnPlan(circuit, self._precision, gemm=kwargs.get("tn_gemm", "fp32"),
+            self._prog = NativeTnPlan(circuit, self._precision, gemm=kwargs.get("tn_gemm", "auto"),
                                       max_rank=kwargs.get("tn_max_rank", 0), repeats=kwargs.get("tn_repeats", 0),
                                       seed=kwargs.get("tn_seed", 0), graphs=kwargs.get("tn_graphs", False))
         else:
