@@ -669,7 +669,9 @@ def run_tn(a):
                              (prog.workspace_bytes(B) / 1e9)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4, "d2h_bytes_per_step": B * 4},
             "gpu_launches": int(per_call),
-            "roofline": {"bound": "tensor", "kernel": "cuBLAS strided-batched GEMM (4M real decomposition)",
+            "roofline": {"bound": "tensor",
+                         "kernel": "contractions: fused in-place kernels (small) + cuBLAS strided-batched GEMMs "
+                                   "(4M real embedding; BF16x9 tensor cores for >= 2^24 flops per circuit)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if peak else None, "traffic": None, "peak_kind": peak_kind,
                          "gemm_ms_per_step": prof.gemm_ms / a.steps, "gather_ms_per_step": prof.gather_ms / a.steps,
