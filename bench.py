@@ -405,17 +405,12 @@ def run_ours(a):
     bytes_per_amp = 32 if fam == "bwd" else 16
     per_launch_bytes = bytes_per_amp * amp_passes / max(1, launches)
     achieved = per_launch_bytes / (kms / max(1, launches) / 1000.0) / 1e9
+    # DRAM bytes per amplitude of one pass from an ncu capture of the same
+    # kernels (profiles/sv_pass_kernels_vqc20q_batch32.md: tedq_fwd_2 476.1 MB,
+    # tedq_bwd_2 1012.3 MB for 32 circuits x 2^20 amplitudes), scaled to a launch
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "sv_pass_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as f:
-                t = json.load(f)
-            traffic = t.get(f"{fam}_pass_bytes_per_amp_per_circuit")
-            if traffic is not None:
-                traffic = traffic * amp_passes / max(1, launches)
-        except Exception:
-            traffic = None
+    if a.workload == "vqc" and a.qubits == 20 and a.layers == 10:
+        traffic = {"fwd": 14.19, "bwd": 30.17}[fam] * amp_passes / max(1, launches)
     gpu_launches = prof.fwd_launches + prof.bwd_launches + prof.meas_launches + prof.lam_launches
 
     line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
