@@ -430,6 +430,32 @@ def run_ours(a):
             "pass_kernels": "generic" if jit_reason else "specialised (NVRTC, sm_103a)",
             "compile_s": round(t_compile, 3),
             "clocks": clk}
+    # accuracy of the complex64 results: against this backend's complex128 path
+    # on the device (8 circuits of the batch) and, unless --no-cpu, against the
+    # complex128 CPU oracle on one circuit (values and gradients)
+    try:
+        k8 = min(8, B) if a.workload != "mbl24" else min(2, B)
+        P8 = params_dev[0][:k8].detach().clone()
+        c128 = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", precision="c128", jit=a.jit)
+        p32 = P8.clone().requires_grad_(True)
+        o32 = cc.execute_batch(p32)
+        loss_of(o32).backward()
+        p64 = P8.double().requires_grad_(True)
+        o64 = c128.execute_batch(p64)
+        loss_of(o64).backward()
+        acc = {"max_abs_err_vs_c128": float((o32.detach().double() - o64.detach()).abs().max()),
+               "max_abs_grad_err_vs_c128": float((p32.grad.double() - p64.grad).abs().max()),
+               "circuits": k8}
+        if not a.no_cpu and a.workload != "mbl24":
+            import oracle
+            z = o64.detach()[0].cpu().double()
+            dy = (2 * z if loss_kind == "sumsq" else torch.ones_like(z)).numpy()
+            v_ref, g_ref = oracle.value_and_grad(spec, P8[0].double().cpu(), dy, torch.complex128)
+            acc["max_abs_err_vs_cpu_c128"] = float((o32.detach()[0].cpu().double() - v_ref.reshape(-1)).abs().max())
+            acc["max_abs_grad_err_vs_cpu_c128"] = float((p32.grad[0].cpu().double() - g_ref).abs().max())
+        line["accuracy"] = acc
+    except Exception as e:  # pragma: no cover
+        line["accuracy"] = {"error": str(e)[:200]}
     if not a.no_plain and a.workload in ("vqc", "small8"):
         try:
             line["plain_gpu_per_circuit"] = {"value": plain_gpu_rate(spec, dev), "unit": UNIT,
