@@ -100,54 +100,71 @@ class _Recorded:
             self.slot_of.append(slots)
         self.n_params = slot
         meas = list(circuit.measurements)
-        M = (_lib.Meas * max(1, len(meas)))()
-        self.layout = []  # per measurement: ("expval", k) | ("probs", off, nq) | ("state",)
+        native = []       # native measurement entries (tedq_meas_t fields)
+        self.layout = []  # per circuit measurement: ("expval", k) | ("var", k, k2) |
+        #                   ("probs", off, nq, m) | ("state",) | ("sample", m)
         k_real = 0
-        for i, m in enumerate(meas):
+
+        def add_expval(obs, square=False):
+            nonlocal k_real
+            F = (_lib.ObsFactor * len(obs))()
+            for j, ob in enumerate(obs):
+                qs = list(ob.qubits)
+                F[j].n_qubits = len(qs)
+                for t, q in enumerate(qs):
+                    F[j].qubits[t] = int(q)
+                if ob.name in _lib.OBS and len(qs) == 1 and not square:
+                    F[j].obs = _lib.OBS[ob.name]
+                else:
+                    mat = np.asarray(ob.matrix, dtype=np.complex128)
+                    arr = _cmatrix(mat @ mat if square else mat, len(qs))
+                    F[j].obs = _lib.OBS_MATRIX
+                    self._keep.append(arr)
+                    F[j].matrix = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            self._keep.append(F)
+            native.append((_lib.MEAS_EXPVAL, F, len(obs), None, 0))
+            k_real += 1
+            return k_real - 1
+
+        for m in meas:
             kind = _kind(m)
+            obs = (m.obs if isinstance(m.obs, list) else [m.obs]) if m.obs is not None else []
             if kind == "expval":
-                obs = m.obs if isinstance(m.obs, list) else [m.obs]
-                F = (_lib.ObsFactor * len(obs))()
-                for j, ob in enumerate(obs):
-                    qs = list(ob.qubits)
-                    F[j].n_qubits = len(qs)
-                    for t, q in enumerate(qs):
-                        F[j].qubits[t] = int(q)
-                    if ob.name in _lib.OBS and len(qs) == 1:
-                        F[j].obs = _lib.OBS[ob.name]
-                    else:
-                        F[j].obs = _lib.OBS_MATRIX
-                        arr = _cmatrix(ob.matrix, len(qs))
-                        self._keep.append(arr)
-                        F[j].matrix = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-                self._keep.append(F)
-                M[i].kind = _lib.MEAS_EXPVAL
-                M[i].n_factors = len(obs)
-                M[i].factors = F
-                self.layout.append(("expval", k_real))
-                k_real += 1
+                self.layout.append(("expval", add_expval(obs)))
+            elif kind == "var":
+                # <O^2> - <O>^2 from two native expectation values
+                self.layout.append(("var", add_expval(obs), add_expval(obs, square=True)))
             elif kind == "probs":
-                M[i].kind = _lib.MEAS_PROBS
                 if m.qubits is None:
-                    M[i].n_qubits = 0
+                    native.append((_lib.MEAS_PROBS, None, 0, None, 0))
                     nq = self.n
                 else:
                     qs = [int(q) for q in m.qubits]
-                    arr = (ctypes.c_int32 * max(1, len(qs)))(*qs)
-                    self._keep.append(arr)
-                    M[i].n_qubits = len(qs)
-                    M[i].qubits = arr
-                    nq = len(set(qs))
                     if len(qs) == 0:
                         raise ValueError("probs(qubits=[]) has no outcome")
+                    arr = (ctypes.c_int32 * max(1, len(qs)))(*qs)
+                    self._keep.append(arr)
+                    native.append((_lib.MEAS_PROBS, None, 0, arr, len(qs)))
+                    nq = len(set(qs))
                 self.layout.append(("probs", k_real, nq, m))
                 k_real += 2 ** nq
             elif kind == "state":
-                M[i].kind = _lib.MEAS_STATE
+                native.append((_lib.MEAS_STATE, None, 0, None, 0))
                 self.layout.append(("state",))
+            elif kind == "sample":
+                self.layout.append(("sample", m))
             else:
                 raise NotImplementedError(f"measurement {kind} is not implemented")
-        self.gates, self.n_ops, self.meas, self.n_meas = gates, len(ops), M, len(meas)
+        M = (_lib.Meas * max(1, len(native)))()
+        for i, (kind, F, nf, qarr, nq) in enumerate(native):
+            M[i].kind = kind
+            if F is not None:
+                M[i].n_factors = nf
+                M[i].factors = F
+            if qarr is not None:
+                M[i].n_qubits = nq
+                M[i].qubits = qarr
+        self.gates, self.n_ops, self.meas, self.n_meas = gates, len(ops), M, len(native)
 
 
 class NativeProgram:
@@ -368,6 +385,70 @@ class GB300ParamShift(torch.autograd.Function):
         return None, grad.to(P.dtype)
 
 
+class _Sampler:
+    """Shots of ``sample`` measurements: a companion program runs the circuit
+    followed by the observables' diagonalising gates and measures the joint
+    probabilities of their qubits on the device; shots are drawn from them on
+    the device (``torch.multinomial``) and mapped to eigenvalue products.
+    Single-qubit Pauli / Hadamard / identity factors."""
+
+    _EIG = {"PauliX": (1.0, -1.0), "PauliY": (1.0, -1.0), "PauliZ": (1.0, -1.0), "Hadamard": (1.0, -1.0),
+            "I": (1.0, 1.0)}
+
+    def __init__(self, circuit, precision, measurements):
+        from .circuit import Circuit
+        from .measurement import probs
+        self.meas = measurements
+        shots = {m.num_shots for m in measurements}
+        if len(shots) != 1:
+            raise ValueError("You can not have multiple measurements with different shapes!!")
+        self.shots = shots.pop()
+        basis, qubits, diag = {}, [], []
+        for m in measurements:
+            for ob in (m.obs if isinstance(m.obs, list) else [m.obs]):
+                if ob.name not in self._EIG or len(ob.qubits) != 1:
+                    raise NotImplementedError(f"sample of {ob.name}: single-qubit Pauli observables only")
+                q = int(ob.qubits[0])
+                if basis.setdefault(q, ob.name) != ob.name:
+                    raise NotImplementedError("sample measurements of different observables on one qubit")
+                if q not in qubits:
+                    qubits.append(q)
+                    for g in ob.diagonalizing_gates():
+                        g._trainable_params = []
+                        diag.append(g)
+        self.qubits = qubits
+        aux = Circuit({"operators": list(circuit.operators) + diag,
+                       "measurements": [probs(qubits=qubits, do_queue=False)],
+                       "init_state": circuit.init_state}, circuit.num_qubits)
+        self.prog = NativeProgram(aux, precision)
+
+    def draw(self, P, ws_cache):
+        prog = self.prog
+        dev, B = P.device, P.shape[0]
+        Pq = P.to(prog.rdtype).contiguous()
+        psi = torch.empty((B, 1 << prog.ns), dtype=prog.cdtype, device=dev)
+        out = torch.empty((B, prog.n_real), dtype=prog.rdtype, device=dev)
+        ws, wsb = ws_cache.get(prog.workspace_bytes(B), dev)
+        with torch.cuda.device(dev):
+            _lib.check(_lib.lib().tedq_run(prog.handle, ctypes.c_void_p(Pq.data_ptr() if Pq.numel() else 0), B,
+                                           ctypes.c_void_p(psi.data_ptr()), ctypes.c_void_p(out.data_ptr()), None,
+                                           ctypes.c_void_p(ws or 0), wsb, _stream_ptr(dev)), "tedq_run")
+        k = len(self.qubits)
+        p = out[:, : 1 << k].double().clamp_min(0.0)
+        idx = torch.multinomial(p, self.shots, replacement=True)  # [B, shots]
+        res = {}
+        for m in self.meas:
+            val = torch.ones_like(idx, dtype=prog.rdtype)
+            for ob in (m.obs if isinstance(m.obs, list) else [m.obs]):
+                pos = self.qubits.index(int(ob.qubits[0]))
+                bit = (idx >> (k - 1 - pos)) & 1
+                e0, e1 = self._EIG[ob.name]
+                val = val * torch.where(bit == 1, torch.tensor(e1, dtype=val.dtype, device=dev),
+                                        torch.tensor(e0, dtype=val.dtype, device=dev))
+            res[id(m)] = val
+        return res
+
+
 class GB300TnExecute(torch.autograd.Function):
     """Tensor-network forward; backward by the parameter-shift rule, all
     shifted networks of a batch contracted as one batch.  (The reference
@@ -444,6 +525,11 @@ class GB300Backend:
         self._device = None
         self._init_dev = None
         self._states_after_measurement = None
+        self._sampler = None
+        self._samples = None
+        if not self._tn and any(item[0] == "sample" for item in self._prog.layout):
+            self._sampler = _Sampler(circuit, self._precision, [it[1] for it in self._prog.layout
+                                                                 if it[0] == "sample"])
 
     # ------------------------------------------------------------ properties
     @property
@@ -602,6 +688,10 @@ class GB300Backend:
         for item in prog.layout:
             if item[0] == "expval":
                 res.append(out[:, item[1]])
+            elif item[0] == "var":
+                res.append(out[:, item[2]] - out[:, item[1]] ** 2)
+            elif item[0] == "sample":
+                res.append(self._samples[id(item[1])])
             elif item[0] == "probs":
                 res.append(out[:, item[1]:item[1] + 2 ** item[2]].reshape([B] + [2] * item[2]))
             else:
@@ -663,6 +753,8 @@ class GB300Backend:
                 with torch.no_grad():
                     return self._forward(Pc.detach())[0]
             return GB300TnExecute.apply(self, Pc)
+        if self._sampler is not None:
+            self._samples = self._sampler.draw(Pc.detach(), self._ws)
         if not self._requires_grad:
             with torch.no_grad():
                 out, psi = self._forward(Pc.detach())

@@ -1,4 +1,4 @@
-"""Measurements: ``expval``, ``probs``, ``state``.
+"""Measurements: ``expval``, ``probs``, ``state``, ``var``, ``sample``.
 
 Mirrors tedq/QInterpreter/operators/measurement.py (``QuantumMeasurement``
 :29-103, ``expval`` :106-155, ``probs`` :174-207, ``state`` :210-237, return
@@ -66,12 +66,29 @@ def expval(observable, do_queue=True):
     return QuantumMeasurement(Expectation, obs=observable, do_queue=do_queue)
 
 
+def _check_obs(observable):
+    for ob in (observable if isinstance(observable, list) else [observable]):
+        if not isinstance(ob, ObservableBase):
+            raise QuantumValueError(f"{ob.name} is not a subclass of ObservableBase: cannot be used here")
+
+
 def var(observable, do_queue=True):
-    raise NotImplementedError
+    """Variance <O^2> - <O>^2 of an observable or tensor product (declared but
+    not implemented by the reference, measurement.py:158-163)."""
+    _check_obs(observable)
+    return QuantumMeasurement(Variance, obs=observable, do_queue=do_queue)
 
 
 def sample(observable, num_shots, do_queue=True):
-    raise NotImplementedError
+    """``num_shots`` eigenvalue samples of an observable or tensor product,
+    drawn from the state's distribution in the observable's eigenbasis
+    (declared but not implemented by the reference, measurement.py:166-171)."""
+    _check_obs(observable)
+    if int(num_shots) < 1:
+        raise QuantumValueError("num_shots must be positive")
+    m = QuantumMeasurement(Sample, obs=observable, do_queue=do_queue)
+    m.num_shots = int(num_shots)
+    return m
 
 
 def probs(qubits=None, do_queue=True, after_state=False):
