@@ -342,69 +342,34 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
           if (rc != TEDQ_OK) return rc;
           continue;
         }
-        // operands of the GEMM: transposing gathers (tile bits chosen so both
-        // the source reads and the operand writes are contiguous)
-        TnTransposeOp G[2];
+        TnGatherArgs A;
+        std::memset(&A, 0, sizeof(A));
         const TnOperand* ops[2] = {&stp.opa, &stp.opb};
         for (int x = 0; x < 2; ++x) {
           const TnOperand& op = *ops[x];
-          TnTransposeOp& o = G[x];
-          TnFusedOp f;
-          fused_op(op, sl, f);  // source pointer, batch stride, slice base, per-bit offsets
-          std::memset(&o, 0, sizeof(o));
-          o.src = f.src;
-          o.src_bstride = f.bstride;
-          o.base = f.base;
-          o.im = f.im;
-          o.nb = net.tensors[op.tensor].batched ? batch : 1;
+          TnGatherOp& o = A.op[x];
+          source(op.tensor, o);
           o.nbits = op.nf + op.nc;
+          if (o.nbits > kTnMaxBits) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
+          for (int j = 0; j < o.nbits; ++j) o.bit[j] = (int8_t)op.src_bit[j];
+          o.base = 0;
+          for (auto& qb : op.slice_bit) o.base += ((sl >> qb.first) & 1) << qb.second;
+          o.nb = net.tensors[op.tensor].batched ? batch : 1;
           o.nc = op.nc;
           o.doubled = op.doubled ? 1 : 0;
-          if (o.nbits > kTnMaxBits) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
-          for (int j = 0; j < op.nc; ++j) o.w[j] = f.wk[j];
-          for (int j = 0; j < op.nf; ++j) o.w[op.nc + j] = f.wf[j];
-          std::vector<int> by_w(o.nbits);
-          for (int j = 0; j < o.nbits; ++j) by_w[j] = j;
-          std::stable_sort(by_w.begin(), by_w.end(), [&](int u, int v) { return o.w[u] < o.w[v]; });
-          const int half = std::min(5, o.nbits);
-          std::vector<char> in_tile(o.nbits, 0);
-          std::vector<int> rd, wr;
-          for (int q = 0; q < half; ++q) {
-            rd.push_back(by_w[q]);
-            in_tile[by_w[q]] = 1;
-          }
-          for (int j = 0; j < half; ++j) {
-            wr.push_back(j);
-            if (!in_tile[j]) {
-              in_tile[j] = 1;
-              rd.push_back(j);
-            }
-          }
-          for (int q = 0; q < half; ++q)
-            if (by_w[q] >= half) wr.push_back(by_w[q]);
-          o.nt = (int)rd.size();
-          for (int q = 0; q < o.nt; ++q) {
-            o.rd[q] = (int8_t)rd[q];
-            o.wr[q] = (int8_t)wr[q];
-            o.r2w[q] = (int8_t)(std::find(wr.begin(), wr.end(), rd[q]) - wr.begin());
-          }
-          for (int j = 0; j < o.nbits; ++j)
-            if (!in_tile[j]) o.ob[o.no++] = (int8_t)j;
         }
-        G[0].dst = scratch;
-        G[1].dst = scratch + ((G[0].doubled ? 4ll : 2ll) << G[0].nbits) * G[0].nb;
+        A.op[0].dst = scratch;
+        A.op[1].dst = scratch + ((A.op[0].doubled ? 4ll : 2ll) << A.op[0].nbits) * A.op[0].nb;
         double gbytes = 0;
-        for (int x = 0; x < 2; ++x)
-          gbytes += (double)G[x].nb * (double)(1ll << G[x].nbits) * sizeof(real) * (G[x].doubled ? 6.0 : 4.0);
+        for (int x = 0; x < 2; ++x) {
+          const TnGatherOp& o = A.op[x];
+          gbytes += (double)o.nb * (double)(1ll << o.nbits) * sizeof(real) * (o.doubled ? 6.0 : 4.0);
+        }
         int32_t rc = timed(p, s, 1, gbytes, [&]() -> int32_t {
-          TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_transpose<real>(G[0], s));
-          TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_transpose<real>(G[1], s));
+          TEDQ_CUDA("tedq_tn_contract: gather kernel", tn_gather<real>(A, s));
           return TEDQ_OK;
         });
         if (rc != TEDQ_OK) return rc;
-        struct {
-          TnTransposeOp op[2];
-        } A = {{G[0], G[1]}};
         const TnTensor& T = net.tensors[stp.out];
         const long long M = 1ll << stp.opa.nf, N = 1ll << stp.opb.nf, K = 1ll << stp.opa.nc;
         real* C = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;

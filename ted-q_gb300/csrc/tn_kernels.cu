@@ -131,55 +131,6 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   }
 }
 
-template <typename real>
-__global__ void __launch_bounds__(256) tn_transpose_kernel(const __grid_constant__ TnTransposeOp o) {
-  __shared__ real sre[1 << kTnTileBits], sim[1 << kTnTileBits];
-  const int nt = o.nt;
-  const int64_t T = 1ll << nt, ntiles = 1ll << o.no;
-  const int64_t n = 1ll << o.nbits, K = 1ll << o.nc;
-  const int64_t dstride = (o.doubled ? 4 : 2) * n;
-  const real* src = static_cast<const real*>(o.src);
-  for (int64_t blk = blockIdx.x; blk < ntiles * o.nb; blk += gridDim.x) {
-    const int64_t b = blk >> o.no, tile = blk & (ntiles - 1);
-    int64_t e0 = 0, s0 = o.base + b * o.src_bstride;
-    for (int q = 0; q < o.no; ++q)
-      if ((tile >> q) & 1) {
-        e0 |= 1ll << o.ob[q];
-        s0 += o.w[o.ob[q]];
-      }
-    for (int64_t i = threadIdx.x; i < T; i += blockDim.x) {
-      int64_t sa = s0;
-      int iw = 0;
-      for (int q = 0; q < nt; ++q)
-        if ((i >> q) & 1) {
-          sa += o.w[o.rd[q]];
-          iw |= 1 << o.r2w[q];
-        }
-      sre[iw] = src[sa];
-      sim[iw] = src[sa + o.im];
-    }
-    __syncthreads();
-    real* d = static_cast<real*>(o.dst) + b * dstride;
-    for (int64_t iw = threadIdx.x; iw < T; iw += blockDim.x) {
-      int64_t e = e0;
-      for (int q = 0; q < nt; ++q)
-        if ((iw >> q) & 1) e |= 1ll << o.wr[q];
-      const int64_t f = e >> o.nc, k = e & (K - 1);
-      real* row = d + f * 2 * K + k;
-      const real re = sre[iw], im = sim[iw];
-      row[0] = re;
-      if (!o.doubled) {
-        row[K] = im;
-      } else {
-        row[K] = -im;
-        row[n * 2] = im;
-        row[n * 2 + K] = re;
-      }
-    }
-    __syncthreads();
-  }
-}
-
 // One thread per (circuit, output element); the contracted-index offsets of
 // both operands are tabulated once per CTA in shared memory.
 template <typename real>
@@ -263,14 +214,6 @@ cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
 }
 
 template <typename real>
-cudaError_t tn_transpose(const TnTransposeOp& op, cudaStream_t stream) {
-  if (op.nt > kTnTileBits || op.nbits > kTnMaxBits) return cudaErrorInvalidValue;
-  int64_t blocks = (1ll << op.no) * op.nb;
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  return launch_kernel(tn_transpose_kernel<real>, dim3((unsigned)blocks), dim3(256), 0, stream, op);
-}
-
-template <typename real>
 cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream) {
   if (args.lk > 8) return cudaErrorInvalidValue;
   const int64_t total = (1ll << (args.lm + args.ln)) * args.nb;
@@ -292,8 +235,6 @@ template cudaError_t tn_build_leaves<double>(const TnLeafDesc*, int, const doubl
                                              cudaStream_t);
 template cudaError_t tn_gather<float>(const TnGatherArgs&, cudaStream_t);
 template cudaError_t tn_gather<double>(const TnGatherArgs&, cudaStream_t);
-template cudaError_t tn_transpose<float>(const TnTransposeOp&, cudaStream_t);
-template cudaError_t tn_transpose<double>(const TnTransposeOp&, cudaStream_t);
 template cudaError_t tn_fused<float>(const TnFusedArgs&, cudaStream_t);
 template cudaError_t tn_fused<double>(const TnFusedArgs&, cudaStream_t);
 template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int, cudaStream_t);

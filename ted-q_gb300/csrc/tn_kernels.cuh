@@ -46,30 +46,6 @@ struct TnGatherArgs {
   TnGatherOp op[2];
 };
 
-// Transposing gather of one GEMM operand (same output as TnGatherOp): the
-// element index e is split into tile bits (at most 10) and outer bits; a CTA
-// reads a tile in source order (tile bits with the smallest source strides
-// lowest) into shared memory and writes it in destination order (the lowest
-// e bits lowest), so both HBM sides are coalesced.
-constexpr int kTnTileBits = 10;
-struct TnTransposeOp {
-  const void* src;
-  void* dst;
-  int64_t src_bstride;          // reals between batch entries of the source (0: shared)
-  int64_t base;                 // reals (slice offset)
-  int64_t im;                   // reals from the real to the imaginary part
-  int64_t nb;                   // batch entries
-  int64_t w[kTnMaxBits];        // source offset (reals) of each e bit
-  int32_t nbits, nc, doubled, nt, no, pad;
-  int8_t rd[kTnTileBits];       // e bit of read-order tile bit q
-  int8_t wr[kTnTileBits];       // e bit of write-order tile bit q
-  int8_t r2w[kTnTileBits];      // write-order position of read-order tile bit q
-  int8_t ob[kTnMaxBits];        // e bit of outer bit q
-};
-
-template <typename real>
-cudaError_t tn_transpose(const TnTransposeOp& op, cudaStream_t stream);
-
 // One operand of a fused contraction, read in place: element (f, k) of the
 // operand's [F][K] view has its real part at src + b * bstride + base +
 // sum_j bit_j(f) * wf[j] + sum_j bit_j(k) * wk[j] (reals) and its imaginary
