@@ -170,46 +170,45 @@ __global__ void __launch_bounds__(kMeasThreads)
   const int64_t circ = circ0 + blockIdx.y;
   const uint64_t N = 1ull << n;
   const cpx<real>* st = psi + circ * (int64_t)N;
-  const uint64_t w0 = (uint64_t)blockIdx.x * kMeasChunk + (uint64_t)tid * 16;
-  const bool valid = w0 < N;
-  cpx<real> v[16];
-  if (valid) {
-    load16<real>(st, w0, v);
-  } else {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) v[j] = mk<real>((real)0, (real)0);
-  }
-  {
-    real h[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) h[j] = v[j].x * v[j].x + v[j].y * v[j].y;
-    wht16<real>(h);
-#pragma unroll
-    for (int j = 0; j < 16; ++j) hs[j][tid] = h[j];
-  }
+  // each thread walks 16-amplitude chunks of its circuit with a grid stride and
+  // keeps FP32 partial sums; one FP64 reduction per CTA and group of 32 strings
+  const uint64_t stride = (uint64_t)gridDim.x * kMeasThreads * 16;
   for (int sg = 0; sg < TT.n; sg += 32) {
-    if (tid < 32) sacc[tid] = 0.0;
-    __syncthreads();
     real part[32];
 #pragma unroll
-    for (int s = 0; s < 32; ++s) {
-      part[s] = 0;
-      if (sg + s < TT.n) {
-        const TermDev& t = TT.t[sg + s];
-        if (t.x == 0) {
-          const real hv = hs[t.z & 15][tid];
-          part[s] = (__popcll(t.z & w0) & 1) ? -hv : hv;
-        } else if (valid) {
-          real q = 0;
-          for (int j = 0; j < 16; ++j) {
-            const uint64_t w = w0 + j;
-            const real tv = term_value<real>(t, v[j], st[w ^ t.x]);
-            q += (__popcll(t.z & w) & 1) ? -tv : tv;
+    for (int s = 0; s < 32; ++s) part[s] = 0;
+    for (uint64_t w0 = ((uint64_t)blockIdx.x * kMeasThreads + tid) * 16; w0 < N; w0 += stride) {
+      cpx<real> v[16];
+      load16<real>(st, w0, v);
+      {
+        real h[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) h[j] = v[j].x * v[j].x + v[j].y * v[j].y;
+        wht16<real>(h);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) hs[j][tid] = h[j];  // own column: no barrier needed
+      }
+#pragma unroll
+      for (int s = 0; s < 32; ++s) {
+        if (sg + s < TT.n) {
+          const TermDev& t = TT.t[sg + s];
+          if (t.x == 0) {
+            const real hv = hs[t.z & 15][tid];
+            part[s] += (__popcll(t.z & w0) & 1) ? -hv : hv;
+          } else {
+            real q = 0;
+            for (int j = 0; j < 16; ++j) {
+              const uint64_t w = w0 + j;
+              const real tv = term_value<real>(t, v[j], st[w ^ t.x]);
+              q += (__popcll(t.z & w) & 1) ? -tv : tv;
+            }
+            part[s] += q;
           }
-          part[s] = q;
         }
       }
     }
+    if (tid < 32) sacc[tid] = 0.0;
+    __syncthreads();
 #pragma unroll
     for (int s = 0; s < 32; ++s) {
       if (sg + s < TT.n) {
@@ -489,7 +488,11 @@ cudaError_t init_impl(int n, int pad, void* psi, const void* init, int64_t batch
 template <typename real>
 cudaError_t expval_impl(int n, const TermTable& TT, const void* psi, double* acc, int64_t batch, cudaStream_t s) {
   const uint64_t N = 1ull << n;
-  const unsigned bx = (unsigned)((N + kMeasChunk - 1) / kMeasChunk);
+  // 16 CTAs per circuit (fewer for small states): each thread sums 16-amplitude
+  // chunks with a grid stride
+  uint64_t bx64 = (N + kMeasChunk - 1) / kMeasChunk;
+  if (bx64 > 16) bx64 = 16;
+  const unsigned bx = (unsigned)bx64;
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     cudaError_t e = launch_kernel(expval_kernel<real>, dim3(bx, (unsigned)nb), dim3(kMeasThreads), 0, s, TT,
@@ -525,7 +528,7 @@ cudaError_t lambda_impl(int n, const TermTable& TT, const ProbsTable& PT, const 
                         int n_real, const void* dys, const void* psi, void* lam, int64_t batch, cudaStream_t s) {
   const uint64_t N = 1ull << n;
   const uint64_t chunks = (N + 16 * 256 - 1) / (16 * 256);
-  const unsigned bx = (unsigned)(chunks < 8192 ? chunks : 8192);
+  const unsigned bx = (unsigned)(chunks < 32 ? chunks : 32);  // grid stride: several chunks per thread
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     cudaError_t e = launch_kernel(lambda_init_kernel<real>, dim3(bx, (unsigned)nb), dim3(256), 0, s, TT, PT, w,
