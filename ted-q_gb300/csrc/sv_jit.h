@@ -42,9 +42,11 @@ struct JitKernels {
 bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSource>& srcs, int n_fwd, int n_bwd,
               JitKernels& out, std::string& err);
 
+// persist: the kernels were generated in the persistent form (grid = resident
+// CTAs, each walking a range of (circuit, tile) items).
 cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
-                           const void* init, int64_t batch, cudaStream_t s);
+                           const void* init, int64_t batch, cudaStream_t s, bool persist);
 cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
-                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s);
+                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s, bool persist);
 
 }  // namespace tedq

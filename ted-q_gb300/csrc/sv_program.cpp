@@ -784,6 +784,14 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   gf.e = gb.e = dbl ? 0 : 1;
   gf.R = dbl ? 4 : 5;
   gb.R = dbl ? 3 : 4;
+  // persistent kernels double-buffer their tile: one bit smaller tiles keep
+  // three CTAs per SM
+  const char* persist_env = getenv("TEDQ_GB300_PERSIST");
+  p->persist = !dbl && persist_env && persist_env[0] == '1';
+  if (p->persist) {
+    mdef_f -= 1;
+    mdef_b -= 1;
+  }
   gf.m = std::min(mdef_f, p->ns);
   gb.m = std::min(mdef_b, p->ns);
   // tuning override "fwd_m,fwd_R,bwd_m,bwd_R" (0 keeps a default); tile and

@@ -62,6 +62,7 @@ struct Program {
   int precision = TEDQ_PREC_C64;
   int fuse = 1;
   int tile_qubits = 0;
+  bool persist = false;  // persistent pass kernels with asynchronous tile prefetch
   std::vector<HGate> elem;    // elementary gates, circuit order
   std::vector<HGate> fused;   // forward gates after fusion
   Schedule fwd, bwd;
