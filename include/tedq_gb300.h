@@ -111,7 +111,12 @@ typedef struct tedq_options {
                           0 = auto (on for states of >= 14 qubits), 1 = on, -1 = off,
                           2 = on in the background (generic kernels until compiled);
                           the environment variable TEDQ_GB300_JIT=0 turns it off   */
-  int32_t reserved[4];
+  int32_t exact_phase; /* 0: uncontrolled diagonal gates (RZ, Z, S, T, ...) drop their
+                          global phase unless the program measures the state (every
+                          output of expval / probs is phase-free, and the adjoint
+                          sweep moves both of its states by the same phase);
+                          1: the final state keeps the exact global phase         */
+  int32_t reserved[3];
 } tedq_options_t;
 
 typedef struct tedq_program tedq_program_t;

@@ -288,7 +288,10 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
     M[0] = cconj(M[0]);
     M[3] = cconj(M[3]);
   }
-  if (md.diag) {
+  if (md.diag == 2) {  // unit-modulus diagonal: d1 / d0 = d1 conj(d0)
+    out[0] = mk<real>((real)1, (real)0);
+    out[1] = cmul(M[3], cconj(M[0]));
+  } else if (md.diag) {
     out[0] = M[0];
     out[1] = M[3];
   } else {

@@ -86,7 +86,8 @@ struct Factor {
 
 // A matrix of a pass: the product F_last ... F_first of its factors.
 struct MatDesc {
-  uint8_t diag;    // 1: the product is diagonal (2 entries), 0: dense 2x2
+  uint8_t diag;    // 0: dense 2x2; 1: diagonal (2 entries); 2: diagonal with its
+                   // global phase dropped, (1, d1 / d0)
   uint8_t nf;      // number of factors
   uint8_t f0;      // first factor index
   uint8_t dagger;  // 1: use the conjugate transpose (adjoint sweep)

@@ -369,8 +369,15 @@ static bool is_hadamard(const HGate& g) {
 
 // Register kind of a gate: structured one-factor rotations and phase-type
 // diagonals get cheaper register code than a dense / general diagonal matrix.
-static uint8_t specialised_kind(const HGate& g) {
+// Uncontrolled diagonal gates whose global phase may be dropped: applied as
+// diag(1, d1 / d0), multiplying only the |1> half.
+static bool phase_droppable(const HGate& g, bool phase_free) {
+  return phase_free && g.kind == GK_D1 && g.cmask == 0;
+}
+
+static uint8_t specialised_kind(const HGate& g, bool phase_free) {
   if (is_hadamard(g)) return GK_H;
+  if (phase_droppable(g, phase_free)) return GK_PH;
   if (g.kind == GK_U1 && g.factors.size() == 1) {
     if (g.factors[0].op == F_RX) return GK_RXT;
     if (g.factors[0].op == F_RY) return GK_RYT;
@@ -410,7 +417,7 @@ struct Cap {
 // kMaxPhases phases are returned in ``rejected`` (they and every gate after
 // them on the same bits go to a later pass).
 static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, const std::vector<HGate>& gl,
-                       const std::vector<int>& taken, bool adjoint, std::vector<int>& rejected) {
+                       const std::vector<int>& taken, bool adjoint, bool phase_free, std::vector<int>& rejected) {
   std::vector<int> tb = sorted_bits(L);
   int pos_of[64];
   for (int i = 0; i < 64; ++i) pos_of[i] = -1;
@@ -540,7 +547,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       const HGate& g = gl[idx];
       RGate& r = P.gate[P.n_gates++];
       memset(&r, 0, sizeof(r));
-      r.kind = specialised_kind(g);
+      r.kind = specialised_kind(g, phase_free);
       r.k0 = (uint8_t)regbit_of[pos_of[g.t0]];
       r.k1 = g.t1 >= 0 ? (uint8_t)regbit_of[pos_of[g.t1]] : 0;
       uint32_t cm = 0;
@@ -557,7 +564,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       if ((g.kind == GK_U1 || g.kind == GK_D1) && r.kind != GK_H) {  // (also RXT / RYT / PH)
         MatDesc& md = P.mat[P.n_mats];
         r.mat = (uint8_t)P.n_mats++;
-        md.diag = g.kind == GK_D1;
+        md.diag = g.kind != GK_D1 ? 0 : (phase_droppable(g, phase_free) ? 2 : 1);
         md.nf = (uint8_t)g.factors.size();
         md.f0 = (uint8_t)P.n_factors;
         md.dagger = adjoint ? 1 : 0;
@@ -580,7 +587,8 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
   }
 }
 
-static Schedule schedule(const std::vector<HGate>& gl, int ns, const Geometry& G, bool adjoint, bool fuse) {
+static Schedule schedule(const std::vector<HGate>& gl, int ns, const Geometry& G, bool adjoint, bool fuse,
+                         bool phase_free) {
   Schedule S;
   std::vector<int> rem(gl.size());
   for (size_t i = 0; i < gl.size(); ++i) rem[i] = (int)i;
@@ -610,7 +618,7 @@ static Schedule schedule(const std::vector<HGate>& gl, int ns, const Geometry& G
     L = fill_bits(L, G.m, ns);
     PassParams P;
     std::vector<int> rejected;
-    build_pass(P, G, ns, L, gl, taken, adjoint, rejected);
+    build_pass(P, G, ns, L, gl, taken, adjoint, phase_free, rejected);
     if (!rejected.empty()) {
       // gates beyond the phase limit go back in circuit order
       std::vector<int> merged = rejected;
@@ -812,9 +820,16 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   }
   gf.c = std::min(4, gf.m);
   gb.c = std::min(4, gb.m);
-  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0);
+  // Global phases: every expval / probs output is invariant under them, and
+  // the adjoint sweep un-applies each gate to both of its states (same phase
+  // on both, so every Im <lambda|G|psi> is unchanged).  Only a state output
+  // (or a caller asking for exact phases) keeps them in the forward passes.
+  bool state_out = opts && opts->exact_phase;
+  for (int i = 0; i < n_meas; ++i) state_out |= meas[i].kind == TEDQ_MEAS_STATE;
+  p->phase_free = !state_out;
+  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free);
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
-  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0);
+  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true);
   compile_measurements(*p, meas, n_meas);
   for (auto& pr : p->probs)
     if ((int)pr.bits.size() < p->n) p->n_probs_bins += 1 << pr.bits.size();

@@ -63,6 +63,7 @@ struct Program {
   int fuse = 1;
   int tile_qubits = 0;
   bool persist = false;  // persistent pass kernels with asynchronous tile prefetch
+  bool phase_free = false;  // forward passes may drop global phases (no state output)
   std::vector<HGate> elem;    // elementary gates, circuit order
   std::vector<HGate> fused;   // forward gates after fusion
   Schedule fwd, bwd;

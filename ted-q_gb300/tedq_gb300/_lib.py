@@ -45,7 +45,7 @@ class Meas(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", c_int32), ("fuse", c_int32), ("tile_qubits", c_int32), ("jit", c_int32),
-                ("reserved", c_int32 * 4)]
+                ("exact_phase", c_int32), ("reserved", c_int32 * 3)]
 
 
 class ProgramInfo(ctypes.Structure):

@@ -170,7 +170,7 @@ class _Recorded:
 class NativeProgram:
     """Owner of one ``tedq_program_t`` (compile of a recorded circuit)."""
 
-    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0, jit=0):
+    def __init__(self, circuit, precision="c64", fuse=True, tile_qubits=0, jit=0, exact_phase=False):
         L = _lib.lib()
         rec = _Recorded(circuit)
         self._rec = rec
@@ -181,6 +181,9 @@ class NativeProgram:
         opts.fuse = 1 if fuse else 0
         opts.tile_qubits = int(tile_qubits)
         opts.jit = int(jit)
+        # post-measurement states are read from the final state: keep its phase
+        after = any(x[0] == "probs" and getattr(x[3], "after_state", False) for x in self.layout)
+        opts.exact_phase = 1 if (exact_phase or after) else 0
         h = ctypes.c_void_p()
         _lib.check(L.tedq_program_create(gates, ops_n, self.n, M, meas_n, ctypes.byref(opts), ctypes.byref(h)),
                    "tedq_program_create")
@@ -520,7 +523,8 @@ class GB300Backend:
                                       seed=kwargs.get("tn_seed", 0), graphs=kwargs.get("tn_graphs", False))
         else:
             self._prog = NativeProgram(circuit, self._precision, fuse=kwargs.get("fuse", True),
-                                       tile_qubits=kwargs.get("tile_qubits", 0), jit=kwargs.get("jit", 0))
+                                       tile_qubits=kwargs.get("tile_qubits", 0), jit=kwargs.get("jit", 0),
+                                       exact_phase=kwargs.get("exact_phase", False))
         self._ws = _Workspace()
         self._device = None
         self._init_dev = None

@@ -54,6 +54,8 @@ def _mats(P, prm):
             M = _factor(F, fixed, prm) @ M
         if md["dagger"]:
             M = M.conj().T
+        if md["diag"] == 2:  # global phase dropped: diag(1, d1 / d0)
+            M = np.diag([1.0, M[1, 1] * np.conj(M[0, 0])])
         out.append(M)
     return out, fixed
 

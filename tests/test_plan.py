@@ -86,12 +86,63 @@ def test_plan_adjoint_matches_reference(case):
     np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=1e-10, rtol=1e-9)
 
 
+def _same_up_to_phase(a, b, atol):
+    ov = np.vdot(b, a)
+    np.testing.assert_allclose(abs(ov), 1.0, atol=atol)
+    np.testing.assert_allclose(a, b * (ov / abs(ov)), atol=atol)
+
+
 def test_plan_unfused_matches_fused():
     case = next(c for c in CASES if c["name"] == "all_gates_n4")
     prm = np.asarray(case["params"], dtype=np.float64)
     a = plan_interp.forward(_compile(case, "c64", fuse=True).describe(), prm)
     b = plan_interp.forward(_compile(case, "c64", fuse=False).describe(), prm)
-    np.testing.assert_allclose(a, b, atol=1e-12)
+    # without a state output, diagonal gates may drop their global phase
+    _same_up_to_phase(a, b, 1e-12)
+
+
+def _phase_case():
+    return {"name": "rz_phase", "n": 3, "init_state": None,
+            "gates": [{"name": "RY", "qubits": [0], "params": [0.3], "trainable": [0]},
+                      {"name": "RZ", "qubits": [0], "params": [0.7], "trainable": [0]},
+                      {"name": "RZ", "qubits": [1], "params": [1.1], "trainable": [0]},
+                      {"name": "T", "qubits": [2], "params": [], "trainable": []},
+                      {"name": "CRZ", "qubits": [0, 2], "params": [0.4], "trainable": [0]},
+                      {"name": "PhaseShift", "qubits": [1], "params": [0.9], "trainable": [0]}],
+            "meas": [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [0]}]}],
+            "params": [0.3, 0.7, 1.1, 0.4, 0.9]}
+
+
+def test_plan_phase_dropping_and_exact_phase():
+    """Uncontrolled diagonal gates drop their global phase only without a
+    state output; exact_phase=1 (and any state measurement) keeps it."""
+    case = _phase_case()
+    circ = qai.Circuit.from_spec(case)
+    free = circ.compilecircuit(backend="gb300", precision="c128").describe()
+    exact = circ.compilecircuit(backend="gb300", precision="c128", exact_phase=True).describe()
+    kinds = lambda d: sorted(md["diag"] for P in d["passes"] for md in P["mats"])
+    assert 2 in kinds(free) and 2 not in kinds(exact)
+    prm = np.asarray(case["params"], dtype=np.float64)
+    a = plan_interp.forward(free, prm)
+    b = plan_interp.forward(exact, prm)
+    _same_up_to_phase(a, b, 1e-12)
+    # the exact program's state is the reference state, phase included
+    import oracle
+    spec = dict(case, meas=[{"kind": "state"}])
+    want = oracle.run(spec, torch.tensor(prm), torch.complex128).numpy().reshape(-1)
+    pad = exact["state_qubits"] - exact["n"]
+    np.testing.assert_allclose(b[:: 1 << pad], want, atol=1e-12)
+    # a state measurement alone also keeps the phase
+    st = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", precision="c128").describe()
+    assert 2 not in kinds(st)
+    # the adjoint sweep always drops it; its gradients still match the reference
+    g = plan_interp.adjoint(circ.compilecircuit(backend="gb300", precision="c128").describe(adjoint=True), prm,
+                            a.copy(), np.ones(free["n_real"]), None)
+    _, want_g = oracle.value_and_grad(case, torch.tensor(prm), [1.0], torch.complex128)
+    np.testing.assert_allclose(g, want_g.numpy(), atol=1e-10)
+
+
+
 
 
 def _hea_spec(n, layers, seed):
