@@ -288,6 +288,14 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
     M[0] = cconj(M[0]);
     M[3] = cconj(M[3]);
   }
+  if (md.diag >= 3) {  // normalised rotation: divide by the larger of |c|, |s|
+    const real c = M[0].x, sn = md.diag == 3 ? -M[1].y : -M[1].x;
+    const bool f0 = fabs(c) >= fabs(sn);
+    out[0] = mk<real>(f0 ? sn / c : c / sn, f0 ? (real)0 : (real)1);
+    out[1] = mk<real>(f0 ? fabs(c) : fabs(sn), (real)0);
+    out[2] = mk<real>((real)1, (real)0);  // running scale: norm_scan
+    return;
+  }
   if (md.diag == 2) {  // unit-modulus diagonal: d1 / d0 = d1 conj(d0)
     out[0] = mk<real>((real)1, (real)0);
     out[1] = cmul(M[3], cconj(M[0]));
@@ -298,6 +306,33 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
     for (int k = 0; k < 4; ++k) out[k] = M[k];
   }
 }
+
+// Running scale of the normalised rotations of a pass: entry [2].x of
+// normalised matrix i becomes the product of the scales of matrices 0..i
+// (matrices are numbered in application order), accumulated in double by
+// warp 0 with a shuffle scan.
+template <typename real>
+__device__ void norm_scan(const PassParams& P, cpx<real> (*mats)[4], int tid) {
+  if (tid >= 32) return;
+  double carry = 1.0;
+  const int n = P.norm_last + 1;
+  for (int base = 0; base < n; base += 32) {
+    const int i = base + tid;
+    const bool on = i < n && P.mat[i].diag >= 3;
+    double v = on ? (double)mats[i][1].x : 1.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_up_sync(0xffffffffu, v, o);
+      if (tid >= o) v *= u;
+    }
+    v *= carry;
+    if (on) mats[i][2].x = (real)v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ real sq(real x) { return x * x; }
 
 // ---------------------------------------------------------------- register gates
 // Complex-array forms (complex128 register sets): bit k of the register index
@@ -397,6 +432,57 @@ __device__ __forceinline__ void apply_h_c(cpx<real>* a, Ctl cm) {
   }
 }
 
+// Normalised rotations (uncontrolled; matrix entries as for GK_RXN / GK_RYN).
+// The form is the same for every thread of the CTA (one circuit): the branch
+// does not diverge.
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_rxn_c(cpx<real>* a, const cpx<real>* M) {
+  const real w = M[0].x;
+  if (M[0].y == (real)0) {  // [[1, -i t], [-i t, 1]]
+#pragma unroll
+    for (int i = 0; i < (1 << R); ++i) {
+      if (i & (1 << K)) continue;
+      const int j = i | (1 << K);
+      const cpx<real> x0 = a[i], x1 = a[j];
+      a[i] = mk<real>(fma(w, x1.y, x0.x), fma(-w, x1.x, x0.y));
+      a[j] = mk<real>(fma(w, x0.y, x1.x), fma(-w, x0.x, x1.y));
+    }
+  } else {  // [[i u, 1], [1, i u]]
+#pragma unroll
+    for (int i = 0; i < (1 << R); ++i) {
+      if (i & (1 << K)) continue;
+      const int j = i | (1 << K);
+      const cpx<real> x0 = a[i], x1 = a[j];
+      a[i] = mk<real>(fma(-w, x0.y, x1.x), fma(w, x0.x, x1.y));
+      a[j] = mk<real>(fma(-w, x1.y, x0.x), fma(w, x1.x, x0.y));
+    }
+  }
+}
+
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_ryn_c(cpx<real>* a, const cpx<real>* M) {
+  const real w = M[0].x;
+  if (M[0].y == (real)0) {  // [[1, -t], [t, 1]]
+#pragma unroll
+    for (int i = 0; i < (1 << R); ++i) {
+      if (i & (1 << K)) continue;
+      const int j = i | (1 << K);
+      const cpx<real> x0 = a[i], x1 = a[j];
+      a[i] = mk<real>(fma(-w, x1.x, x0.x), fma(-w, x1.y, x0.y));
+      a[j] = mk<real>(fma(w, x0.x, x1.x), fma(w, x0.y, x1.y));
+    }
+  } else {  // [[u, -1], [1, u]]
+#pragma unroll
+    for (int i = 0; i < (1 << R); ++i) {
+      if (i & (1 << K)) continue;
+      const int j = i | (1 << K);
+      const cpx<real> x0 = a[i], x1 = a[j];
+      a[i] = mk<real>(fma(w, x0.x, -x1.x), fma(w, x0.y, -x1.y));
+      a[j] = mk<real>(fma(w, x1.x, x0.x), fma(w, x1.y, x0.y));
+    }
+  }
+}
+
 // Per-thread part of Im <lambda| G |psi> on the control subspace
 // (G = X, Y, Z or P1 = |1><1| on register bit K).
 template <int G, int K, int R, typename real, typename Ctl>
@@ -419,6 +505,19 @@ __device__ __forceinline__ real grad_part_c(const cpx<real>* p, const cpx<real>*
 template <int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ void apply_u1(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
   apply_u1_c<K, R, double>(A.a, M, cm);
+}
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_rxn(Regs<double, R>& A, const cpx<double>* M) {
+  apply_rxn_c<K, R, double>(A.a, M);
+}
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_ryn(Regs<double, R>& A, const cpx<double>* M) {
+  apply_ryn_c<K, R, double>(A.a, M);
+}
+template <int R>
+__device__ __forceinline__ void rescale(Regs<double, R>& A, double k) {
+#pragma unroll
+  for (int i = 0; i < (1 << R); ++i) A.a[i] = mk<double>(k * A.a[i].x, k * A.a[i].y);
 }
 template <int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ void apply_d1(Regs<double, R>& A, const cpx<double>* M, Ctl cm) {
@@ -590,6 +689,113 @@ __device__ __forceinline__ void apply_ryt(Regs<float, R>& A, const cpx<float>* M
   }
 }
 
+// Normalised rotations on packed registers: one FFMA2 per float2 component.
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_rxn(Regs<float, R>& A, const cpx<float>* M) {
+  constexpr int NG = 1 << (R - 1);
+  const float2 W = bc2(M[0].x), NW = bc2(-M[0].x);
+  if (M[0].y == 0.f) {  // [[1, -i t], [-i t, 1]]
+    if constexpr (K == 0) {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        const float2 xr = A.re[g], xi = A.im[g];
+        A.re[g] = fma2(W, swp(xi), xr);
+        A.im[g] = fma2(NW, swp(xr), xi);
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        if (g & (1 << (K - 1))) continue;
+        const int h = g | (1 << (K - 1));
+        const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+        A.re[g] = fma2(W, xi1, xr0);
+        A.im[g] = fma2(NW, xr1, xi0);
+        A.re[h] = fma2(W, xi0, xr1);
+        A.im[h] = fma2(NW, xr0, xi1);
+      }
+    }
+  } else {  // [[i u, 1], [1, i u]]
+    if constexpr (K == 0) {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        const float2 xr = A.re[g], xi = A.im[g];
+        A.re[g] = fma2(NW, xi, swp(xr));
+        A.im[g] = fma2(W, xr, swp(xi));
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        if (g & (1 << (K - 1))) continue;
+        const int h = g | (1 << (K - 1));
+        const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+        A.re[g] = fma2(NW, xi0, xr1);
+        A.im[g] = fma2(W, xr0, xi1);
+        A.re[h] = fma2(NW, xi1, xr0);
+        A.im[h] = fma2(W, xr1, xi0);
+      }
+    }
+  }
+}
+
+template <int K, int R, typename real>
+__device__ __forceinline__ void apply_ryn(Regs<float, R>& A, const cpx<float>* M) {
+  constexpr int NG = 1 << (R - 1);
+  const float w = M[0].x;
+  const float2 W = bc2(w), NW = bc2(-w);
+  if (M[0].y == 0.f) {  // [[1, -t], [t, 1]]
+    if constexpr (K == 0) {
+      const float2 V = make_float2(-w, w);
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        A.re[g] = fma2(V, swp(A.re[g]), A.re[g]);
+        A.im[g] = fma2(V, swp(A.im[g]), A.im[g]);
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        if (g & (1 << (K - 1))) continue;
+        const int h = g | (1 << (K - 1));
+        const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+        A.re[g] = fma2(NW, xr1, xr0);
+        A.im[g] = fma2(NW, xi1, xi0);
+        A.re[h] = fma2(W, xr0, xr1);
+        A.im[h] = fma2(W, xi0, xi1);
+      }
+    }
+  } else {  // [[u, -1], [1, u]]
+    if constexpr (K == 0) {
+      const float2 V = make_float2(-1.f, 1.f);
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        A.re[g] = fma2(V, swp(A.re[g]), mul2(W, A.re[g]));
+        A.im[g] = fma2(V, swp(A.im[g]), mul2(W, A.im[g]));
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        if (g & (1 << (K - 1))) continue;
+        const int h = g | (1 << (K - 1));
+        const float2 xr0 = A.re[g], xi0 = A.im[g], xr1 = A.re[h], xi1 = A.im[h];
+        A.re[g] = fma2(W, xr0, make_float2(-xr1.x, -xr1.y));
+        A.im[g] = fma2(W, xi0, make_float2(-xi1.x, -xi1.y));
+        A.re[h] = fma2(W, xr1, xr0);
+        A.im[h] = fma2(W, xi1, xi0);
+      }
+    }
+  }
+}
+
+// Multiply a register set by the pass's scale (after its last normalised gate).
+template <int R>
+__device__ __forceinline__ void rescale(Regs<float, R>& A, float k) {
+  const float2 K2 = bc2(k);
+#pragma unroll
+  for (int g = 0; g < (1 << (R - 1)); ++g) {
+    A.re[g] = mul2(K2, A.re[g]);
+    A.im[g] = mul2(K2, A.im[g]);
+  }
+}
+
 template <int K, int R, typename real, typename Ctl>
 __device__ __forceinline__ void apply_ph(Regs<float, R>& A, const cpx<float>* M, Ctl cm) {
   TEDQ_GROUPS
@@ -729,6 +935,8 @@ __device__ __forceinline__ void dispatch_gate(int kind, int k, Regs<real, R>& a,
         case GK_RYT: apply_ryt<K, R, real>(a, M, cm); break;
         case GK_PH: apply_ph<K, R, real>(a, M, cm); break;
         case GK_H: apply_h<K, R, real>(a, cm); break;
+        case GK_RXN: apply_rxn<K, R, real>(a, M); break;
+        case GK_RYN: apply_ryn<K, R, real>(a, M); break;
         default: apply_x<K, R, real>(a, cm); break;
       }
     } else {
@@ -887,13 +1095,18 @@ struct FwdPass {
     const int64_t circ = circ0 + blockIdx.y;
     st = psi + (circ << P.n);
     const real* prm = params ? params + circ * n_params : nullptr;
-    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
     gthr = tile_base(P, blockIdx.x);
     sthr = 0;
     thread_offsets(P, tid, P.m - R, gthr, sthr);
     U v[NU];
 #pragma unroll
     for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
+    // matrices while the tile loads are in flight
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
+    if (P.norm_last != kNoNorm) {
+      __syncthreads();
+      norm_scan<real>(P, mats, tid);
+    }
 #pragma unroll
     for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = to_s(v[k]);
     __syncthreads();
@@ -966,6 +1179,10 @@ struct BwdPass {
     sl = lam + (circ << P.n);
     const real* prm = params ? params + circ * n_params : nullptr;
     for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
+    if (P.norm_last != kNoNorm) {
+      __syncthreads();
+      norm_scan<real>(P, mats, tid);
+    }
     gthr = tile_base(P, blockIdx.x);
     sthr = 0;
     thread_offsets(P, tid, P.m - R, gthr, sthr);

@@ -51,6 +51,12 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
       snprintf(buf, sizeof buf, "  apply_h<%d, %d, %s>(%s, CM<%s>{});\n", r.k0, R, real, arr, cm(r.cmask).c_str());
       o << buf;
       break;
+    case GK_RXN:
+    case GK_RYN:
+      snprintf(buf, sizeof buf, "  %s<%d, %d, %s>(%s, c.mats[%d]);\n", r.kind == GK_RXN ? "apply_rxn" : "apply_ryn",
+               r.k0, R, real, arr, r.mat);
+      o << buf;
+      break;
     default: {  // GK_SWAP as three controlled bit flips
       const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
       const int tg[3] = {r.k1, r.k0, r.k1};
@@ -115,6 +121,7 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
     o << ");\n";
     pending.clear();
   };
+  int kap = -1;  // last normalised matrix applied (its [2].x = scale so far)
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
     if (ph.type != PH_REG) {
@@ -127,16 +134,28 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
       if (adjoint && r.grad != GR_NONE) {
         static const char* gn[] = {"", "GR_X", "GR_Y", "GR_Z", "GR_P1"};
         const std::string v = "gv" + std::to_string(var++);
-        snprintf(buf, sizeof buf, "  const %s %s = grad_part<%s, %d, %d, %s>(c.a, c.l, CM<%uu>{});\n", real,
-                 v.c_str(), gn[r.grad], r.k0, P.R, real, (unsigned)r.cmask);
+        // both states carry 1 / (scale so far): the product carries its square
+        const std::string k2 = kap < 0 ? "" : " * sq(c.mats[" + std::to_string(kap) + "][2].x)";
+        // the empty asm pins the partial here: otherwise the compiler may sink
+        // it towards grad8 and keep old copies of both states alive
+        snprintf(buf, sizeof buf,
+                 "  %s %s = grad_part<%s, %d, %d, %s>(c.a, c.l, CM<%uu>{})%s;\n  asm volatile(\"\" : \"+%s\"(%s));\n",
+                 real, v.c_str(), gn[r.grad], r.k0, P.R, real, (unsigned)r.cmask, k2.c_str(), P.e == 1 ? "f" : "d",
+                 v.c_str());
         o << buf;
         pending.push_back({v, g});
         if (pending.size() == 8) flush();
       }
       emit_gate(o, P, r, "c.a");
       if (adjoint) emit_gate(o, P, r, "c.l");
+      if (r.kind == GK_RXN || r.kind == GK_RYN) kap = r.mat;
     }
     flush();
+    if (f == P.norm_phase) {
+      o << "  rescale<" << (int)P.R << ">(c.a, c.mats[" << (int)P.norm_last << "][2].x);\n";
+      if (adjoint) o << "  rescale<" << (int)P.R << ">(c.l, c.mats[" << (int)P.norm_last << "][2].x);\n";
+      kap = -1;
+    }
     o << "  c.end(" << f << ");\n";
   }
   o << (persist ? "  c.finish();\n  }\n}\n\n" : "  c.finish();\n}\n\n");
@@ -266,6 +285,10 @@ bool jit_compile(const std::string& src, std::string& cubin, std::string& err) {
       cubin = ss.str();
       if (!cubin.empty()) return true;
     }
+  }
+  if (const char* dump = getenv("TEDQ_GB300_JIT_DUMP")) {  // generated source, for inspection
+    mkdirs(dump);
+    std::ofstream(std::string(dump) + name + ".cu") << src;
   }
   nvrtcProgram prog;
   nvrtcResult r = N.create(&prog, src.c_str(), "tedq_passes.cu", 2, kJitHeaderSrc, kJitHeaderNames);

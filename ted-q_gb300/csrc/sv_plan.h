@@ -49,7 +49,18 @@ enum GateKind : uint8_t {
   GK_RYT = 5,   // [[c, -s], [s, c]]:      c = M[0].re, s = -M[1].re
   GK_PH = 6,    // diag(1, d): only the |1> half is multiplied (d = matrix entry 1)
   GK_H = 7,     // Hadamard (x0 + x1, x0 - x1) / sqrt(2) (no matrix)
+  // Normalised rotations (global phase and scale dropped; uncontrolled only):
+  // the gate divided by the larger of |c|, |s| costs one FMA per real
+  // component.  Matrix entries: [0] = (coefficient, form), [1] = (scale, 0),
+  // [2] = (running scale product of the pass up to this gate, 0).
+  //   RXN form 0: [[1, -i t], [-i t, 1]]   form 1: [[i u, 1], [1, i u]]
+  //   RYN form 0: [[1, -t], [t, 1]]        form 1: [[u, -1], [1, u]]
+  // The pass multiplies its states by the total scale after the last one.
+  GK_RXN = 8,
+  GK_RYN = 9,
 };
+
+constexpr uint8_t kNoNorm = 0xFF;
 
 // Generator kinds of the adjoint gradient: the gradient of a gate
 // U(theta) with dU/dtheta = K U is 2 Re <lambda| K |psi> evaluated on the
@@ -87,7 +98,8 @@ struct Factor {
 // A matrix of a pass: the product F_last ... F_first of its factors.
 struct MatDesc {
   uint8_t diag;    // 0: dense 2x2; 1: diagonal (2 entries); 2: diagonal with its
-                   // global phase dropped, (1, d1 / d0)
+                   // global phase dropped, (1, d1 / d0); 3 / 4: normalised RX- /
+                   // RY-type rotation (GK_RXN / GK_RYN entries)
   uint8_t nf;      // number of factors
   uint8_t f0;      // first factor index
   uint8_t dagger;  // 1: use the conjugate transpose (adjoint sweep)
@@ -128,7 +140,10 @@ struct PassParams {
   uint16_t n_gates, n_mats, n_factors, n_grad;
   uint8_t pad_bits;  // init == 2: low idle qubits added by padding
   uint8_t lam_init;  // adjoint: first pass builds lambda from psi in-kernel
-  uint8_t pad[2];
+  // normalised rotations: matrix of the last one (kNoNorm = none) and the
+  // register phase whose end multiplies the states by the pass's scale
+  uint8_t norm_last;
+  uint8_t norm_phase;
   uint8_t hi[kMaxTileBits];      // global bit of tile bit c+i
   uint8_t outer[kMaxStateBits];  // global bit of outer-index bit i
   // Tile staging: thread tid stages units u = tid + k * 2^(m-R), k < 2^(R-e).

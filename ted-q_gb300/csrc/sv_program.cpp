@@ -303,8 +303,28 @@ static void lower_gate(const tedq_gate_t& g, int n, int ns, std::vector<HGate>& 
 
 // ---------------------------------------------------------------- fusion
 
-static std::vector<HGate> fuse_one_qubit_runs(const std::vector<HGate>& in, int ns) {
+static bool is_hadamard(const HGate& g);
+static uint8_t normalised_kind(const HGate& g, bool norm);
+static uint8_t specialised_kind(const HGate& g, bool phase_free, bool norm);
+
+// Register-phase cost of a gate (packed FP32x2 instructions per amplitude of
+// one state): the fused form is kept only where it is cheaper than its parts.
+static int gate_cost(const HGate& g, bool norm) {
+  if (g.kind == GK_X || g.kind == GK_SWAP) return 0;
+  if (normalised_kind(g, norm)) return 1;
+  if (g.kind == GK_D1) return (norm && g.cmask == 0) || specialised_kind(g, false, false) == GK_PH ? 1 : 2;
+  if (is_hadamard(g)) return 2;
+  if (g.factors.size() == 1 && (g.factors[0].op == F_RX || g.factors[0].op == F_RY)) return 2;
+  return 4;
+}
+
+// Runs of uncontrolled one-qubit gates on the same qubit become one gate
+// (product of their factors).  With normalised rotations (norm: the forward
+// passes may drop global phases) a run whose parts cost less than the fused
+// matrix stays unfused, e.g. RX RY RZ = 1 + 1 + 1 against 4 for a dense 2x2.
+static std::vector<HGate> fuse_one_qubit_runs(const std::vector<HGate>& in, int ns, bool norm) {
   std::vector<HGate> out;
+  std::vector<std::vector<HGate>> parts;  // source gates of out[i]
   std::vector<int> last(ns, -1);
   const size_t kMaxRun = 8;
   for (const HGate& g : in) {
@@ -329,16 +349,30 @@ static std::vector<HGate> fuse_one_qubit_runs(const std::vector<HGate>& in, int 
           f.kind = all_diag ? GK_D1 : GK_U1;
           f.grad = GR_NONE;
           f.slot = -1;
+          parts[j].push_back(g);
           continue;
         }
       }
     }
     out.push_back(g);
+    parts.push_back({g});
     uint64_t b = g.bits();
     for (int i = 0; i < ns; ++i)
       if (b >> i & 1) last[i] = (int)out.size() - 1;
   }
-  return out;
+  if (!norm) return out;
+  // the parts of a run act on one qubit with nothing else on it in between:
+  // they may replace the fused gate at its position
+  std::vector<HGate> res;
+  for (size_t i = 0; i < out.size(); ++i) {
+    int sum = 0;
+    for (const HGate& q : parts[i]) sum += gate_cost(q, true);
+    if (parts[i].size() > 1 && sum < gate_cost(out[i], true))
+      res.insert(res.end(), parts[i].begin(), parts[i].end());
+    else
+      res.push_back(out[i]);
+  }
+  return res;
 }
 
 // ---------------------------------------------------------------- scheduling
@@ -375,8 +409,17 @@ static bool phase_droppable(const HGate& g, bool phase_free) {
   return phase_free && g.kind == GK_D1 && g.cmask == 0;
 }
 
-static uint8_t specialised_kind(const HGate& g, bool phase_free) {
+// Uncontrolled one-factor RX / RY gates that run normalised (GK_RXN / GK_RYN).
+static uint8_t normalised_kind(const HGate& g, bool norm) {
+  if (!norm || g.kind != GK_U1 || g.cmask != 0 || g.factors.size() != 1) return 0;
+  if (g.factors[0].op == F_RX) return GK_RXN;
+  if (g.factors[0].op == F_RY) return GK_RYN;
+  return 0;
+}
+
+static uint8_t specialised_kind(const HGate& g, bool phase_free, bool norm) {
   if (is_hadamard(g)) return GK_H;
+  if (const uint8_t k = normalised_kind(g, phase_free && norm)) return k;
   if (phase_droppable(g, phase_free)) return GK_PH;
   if (g.kind == GK_U1 && g.factors.size() == 1) {
     if (g.factors[0].op == F_RX) return GK_RXT;
@@ -417,7 +460,8 @@ struct Cap {
 // kMaxPhases phases are returned in ``rejected`` (they and every gate after
 // them on the same bits go to a later pass).
 static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, const std::vector<HGate>& gl,
-                       const std::vector<int>& taken, bool adjoint, bool phase_free, std::vector<int>& rejected) {
+                       const std::vector<int>& taken, bool adjoint, bool phase_free, bool norm,
+                       std::vector<int>& rejected) {
   std::vector<int> tb = sorted_bits(L);
   int pos_of[64];
   for (int i = 0; i < 64; ++i) pos_of[i] = -1;
@@ -429,6 +473,8 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
     return t;
   };
   memset(&P, 0, sizeof(P));
+  P.norm_last = kNoNorm;
+  P.norm_phase = kNoNorm;
   P.m = (uint8_t)G.m;
   P.c = (uint8_t)G.c;
   P.e = (uint8_t)G.e;
@@ -547,7 +593,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       const HGate& g = gl[idx];
       RGate& r = P.gate[P.n_gates++];
       memset(&r, 0, sizeof(r));
-      r.kind = specialised_kind(g, phase_free);
+      r.kind = specialised_kind(g, phase_free, norm);
       r.k0 = (uint8_t)regbit_of[pos_of[g.t0]];
       r.k1 = g.t1 >= 0 ? (uint8_t)regbit_of[pos_of[g.t1]] : 0;
       uint32_t cm = 0;
@@ -565,6 +611,11 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
         MatDesc& md = P.mat[P.n_mats];
         r.mat = (uint8_t)P.n_mats++;
         md.diag = g.kind != GK_D1 ? 0 : (phase_droppable(g, phase_free) ? 2 : 1);
+        if (r.kind == GK_RXN || r.kind == GK_RYN) {
+          md.diag = r.kind == GK_RXN ? 3 : 4;
+          P.norm_last = r.mat;
+          P.norm_phase = P.n_phases;
+        }
         md.nf = (uint8_t)g.factors.size();
         md.f0 = (uint8_t)P.n_factors;
         md.dagger = adjoint ? 1 : 0;
@@ -588,7 +639,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
 }
 
 static Schedule schedule(const std::vector<HGate>& gl, int ns, const Geometry& G, bool adjoint, bool fuse,
-                         bool phase_free) {
+                         bool phase_free, bool norm) {
   Schedule S;
   std::vector<int> rem(gl.size());
   for (size_t i = 0; i < gl.size(); ++i) rem[i] = (int)i;
@@ -618,7 +669,7 @@ static Schedule schedule(const std::vector<HGate>& gl, int ns, const Geometry& G
     L = fill_bits(L, G.m, ns);
     PassParams P;
     std::vector<int> rejected;
-    build_pass(P, G, ns, L, gl, taken, adjoint, phase_free, rejected);
+    build_pass(P, G, ns, L, gl, taken, adjoint, phase_free, norm, rejected);
     if (!rejected.empty()) {
       // gates beyond the phase limit go back in circuit order
       std::vector<int> merged = rejected;
@@ -785,7 +836,7 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
     for (int j = 0; j < np; ++j) max_slot = std::max(max_slot, (int)gates[i].param_slot[j]);
   }
   p->n_params = max_slot + 1;
-  p->fused = p->fuse ? fuse_one_qubit_runs(p->elem, p->ns) : p->elem;
+  p->fused = p->elem;  // fused below, once the register-gate forms are known
   Geometry gf, gb;
   int mdef_f = dbl ? 12 : 13, mdef_b = dbl ? 11 : 12;
   if (p->tile_qubits > 0) mdef_f = std::min(mdef_f, std::max(p->tile_qubits, 6));
@@ -827,9 +878,14 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   bool state_out = opts && opts->exact_phase;
   for (int i = 0; i < n_meas; ++i) state_out |= meas[i].kind == TEDQ_MEAS_STATE;
   p->phase_free = !state_out;
-  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free);
+  // normalised rotations (one FMA per component; the persistent kernels do
+  // not track the pass scale); TEDQ_GB300_NORMALISE=0 turns them off (tuning)
+  const char* norm_env = getenv("TEDQ_GB300_NORMALISE");
+  p->normalise = !p->persist && !(norm_env && norm_env[0] == '0');
+  if (p->fuse) p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && p->normalise);
+  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, p->normalise);
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
-  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true);
+  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, p->normalise);
   compile_measurements(*p, meas, n_meas);
   for (auto& pr : p->probs)
     if ((int)pr.bits.size() < p->n) p->n_probs_bins += 1 << pr.bits.size();
@@ -858,7 +914,9 @@ std::string describe_schedule(const Program& p, bool adjoint) {
     for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << P.gk[j];
     o << "],\"sk\":[";
     for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << P.sk[j];
-    o << "],\"phases\":[";
+    o << "],\"norm_last\":" << (P.norm_last == kNoNorm ? -1 : (int)P.norm_last)
+      << ",\"norm_phase\":" << (P.norm_phase == kNoNorm ? -1 : (int)P.norm_phase);
+    o << ",\"phases\":[";
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];
       if (f) o << ",";

@@ -12,7 +12,7 @@ lowering and the Pauli expansion of the observables without a GPU.
 import numpy as np
 
 F_FIXED2, F_FIXD, F_RX, F_RY, F_RZ, F_PHASE, F_ROT = range(7)
-GK_U1, GK_D1, GK_X, GK_SWAP, GK_RXT, GK_RYT, GK_PH, GK_H = range(8)
+GK_U1, GK_D1, GK_X, GK_SWAP, GK_RXT, GK_RYT, GK_PH, GK_H, GK_RXN, GK_RYN = range(10)
 GR_NONE, GR_X, GR_Y, GR_Z, GR_P1 = range(5)
 
 
@@ -45,19 +45,37 @@ def _factor(F, fixed, prm):
     raise ValueError(op)
 
 
+def _normalised(M, rx):
+    """Normalised rotation (GK_RXN / GK_RYN): the gate divided by the larger
+    of |c|, |s| with its global phase dropped; returns (matrix, scale)."""
+    c = M[0, 0].real
+    s = -M[0, 1].imag if rx else -M[0, 1].real
+    if abs(c) >= abs(s):
+        t = s / c
+        N = np.array([[1, -1j * t], [-1j * t, 1]]) if rx else np.array([[1, -t], [t, 1]], dtype=complex)
+        return N, abs(c)
+    u = c / s
+    N = np.array([[1j * u, 1], [1, 1j * u]]) if rx else np.array([[u, -1], [1, u]], dtype=complex)
+    return N, abs(s)
+
+
 def _mats(P, prm):
     fixed = [complex(a, b) for a, b in P["fixed"]]
-    out = []
+    out, sig = [], []
     for md in P["mats"]:
         M = np.eye(2, dtype=complex)
         for F in md["factors"]:
             M = _factor(F, fixed, prm) @ M
         if md["dagger"]:
             M = M.conj().T
+        sg = 1.0
         if md["diag"] == 2:  # global phase dropped: diag(1, d1 / d0)
             M = np.diag([1.0, M[1, 1] * np.conj(M[0, 0])])
+        elif md["diag"] >= 3:
+            M, sg = _normalised(M, md["diag"] == 3)
         out.append(M)
-    return out, fixed
+        sig.append(sg)
+    return out, fixed, sig
 
 
 def _apply(a, r, M):
@@ -82,6 +100,8 @@ def _apply(a, r, M):
         kind = GK_D1
     elif kind == GK_H:
         M = np.array([[1.0, 1.0], [1.0, -1.0]], dtype=complex) / np.sqrt(2.0)
+        kind = GK_U1
+    elif kind in (GK_RXN, GK_RYN):
         kind = GK_U1
     for i in range(NR):
         if kind == GK_D1:
@@ -158,7 +178,7 @@ def _tile_index(P, tile):
 
 def run_pass(P, psi, prm, lam=None, grads=None):
     m, e, R = P["m"], P["e"], P["R"]
-    mats, fixed = _mats(P, prm)
+    mats, fixed, sig = _mats(P, prm)
     n_outer = len(P["outer"])
     T = 1 << (m - R)
     phys = np.array([(swz_unit(t >> e) << e) | (t & ((1 << e) - 1)) for t in range(1 << m)])
@@ -170,7 +190,8 @@ def run_pass(P, psi, prm, lam=None, grads=None):
         if lam is not None:
             tl = np.zeros(1 << m, dtype=complex)
             tl[phys] = lam[g]
-        for ph in P["phases"]:
+        kap = 1.0  # states carry 1 / (product of normalised-rotation scales so far)
+        for f, ph in enumerate(P["phases"]):
             if ph["type"] == 1:
                 _dense(tp, P, ph, fixed, m, e)
                 if tl is not None:
@@ -190,10 +211,17 @@ def run_pass(P, psi, prm, lam=None, grads=None):
             for r in ph["gates"]:
                 M = mats[r["mat"]] if r["kind"] not in (GK_X, GK_SWAP, GK_H) else None
                 if l is not None and r["grad"] != GR_NONE:
-                    grads[r["slot"]] += _grad(a, l, r)
+                    grads[r["slot"]] += _grad(a, l, r) * kap * kap
                 _apply(a, r, M)
                 if l is not None:
                     _apply(l, r, M)
+                if r["kind"] in (GK_RXN, GK_RYN):
+                    kap *= sig[r["mat"]]
+            if f == P.get("norm_phase", -1):
+                a *= kap
+                if l is not None:
+                    l *= kap
+                kap = 1.0
             tp[addr] = a
             if tl is not None:
                 tl[addr] = l
