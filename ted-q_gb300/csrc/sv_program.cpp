@@ -309,9 +309,12 @@ static uint8_t specialised_kind(const HGate& g, bool phase_free, bool norm);
 
 // Register-phase cost of a gate (packed FP32x2 instructions per amplitude of
 // one state): the fused form is kept only where it is cheaper than its parts.
+// A normalised rotation counts as 2: it executes one FFMA2 per component but
+// carries the code of both of its forms, and measured runs of RX RY RZ ran
+// faster fused (the pass kernels are sensitive to code size).
 static int gate_cost(const HGate& g, bool norm) {
   if (g.kind == GK_X || g.kind == GK_SWAP) return 0;
-  if (normalised_kind(g, norm)) return 1;
+  if (normalised_kind(g, norm)) return 2;
   if (g.kind == GK_D1) return (norm && g.cmask == 0) || specialised_kind(g, false, false) == GK_PH ? 1 : 2;
   if (is_hadamard(g)) return 2;
   if (g.factors.size() == 1 && (g.factors[0].op == F_RX || g.factors[0].op == F_RY)) return 2;
@@ -321,7 +324,7 @@ static int gate_cost(const HGate& g, bool norm) {
 // Runs of uncontrolled one-qubit gates on the same qubit become one gate
 // (product of their factors).  With normalised rotations (norm: the forward
 // passes may drop global phases) a run whose parts cost less than the fused
-// matrix stays unfused, e.g. RX RY RZ = 1 + 1 + 1 against 4 for a dense 2x2.
+// matrix stays unfused, e.g. RZ H = 1 + 2 against 4 for a dense 2x2.
 static std::vector<HGate> fuse_one_qubit_runs(const std::vector<HGate>& in, int ns, bool norm) {
   std::vector<HGate> out;
   std::vector<std::vector<HGate>> parts;  // source gates of out[i]
@@ -879,13 +882,18 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   for (int i = 0; i < n_meas; ++i) state_out |= meas[i].kind == TEDQ_MEAS_STATE;
   p->phase_free = !state_out;
   // normalised rotations (one FMA per component; the persistent kernels do
-  // not track the pass scale); TEDQ_GB300_NORMALISE=0 turns them off (tuning)
+  // not track the pass scale).  Tuning: TEDQ_GB300_NORMALISE holds the
+  // letters f (forward passes), b (adjoint passes), u (runs of one-qubit
+  // gates stay unfused where their normalised parts cost less); "0" = none.
   const char* norm_env = getenv("TEDQ_GB300_NORMALISE");
-  p->normalise = !p->persist && !(norm_env && norm_env[0] == '0');
-  if (p->fuse) p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && p->normalise);
-  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, p->normalise);
+  const std::string norm_opt = norm_env ? norm_env : "fbu";
+  const bool norm_f = norm_opt.find('f') != std::string::npos, norm_b = norm_opt.find('b') != std::string::npos,
+             norm_u = norm_opt.find('u') != std::string::npos;
+  p->normalise = !p->persist && (norm_f || norm_b);
+  if (p->fuse) p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && !p->persist && norm_f && norm_u);
+  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, !p->persist && norm_f);
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
-  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, p->normalise);
+  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, !p->persist && norm_b);
   compile_measurements(*p, meas, n_meas);
   for (auto& pr : p->probs)
     if ((int)pr.bits.size() < p->n) p->n_probs_bins += 1 << pr.bits.size();

@@ -162,3 +162,27 @@ def test_unfused_equals_fused():
     b = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False, fuse=False)
     params = torch.rand(4, a.num_params, device=DEV) * 6.28
     torch.testing.assert_close(a.execute_batch(params), b.execute_batch(params), atol=2e-6, rtol=1e-5)
+
+
+@pytest.mark.parametrize("norm", ["0", "f", "fbu"])
+@pytest.mark.parametrize("jit", [-1, 1], ids=["generic", "specialised"])
+def test_register_gate_forms(monkeypatch, norm, jit):
+    """Value and adjoint gradient with each choice of register-gate forms
+    (plain rotations, normalised rotations in the forward passes only, and
+    normalised rotations everywhere with cost-based unfusing)."""
+    monkeypatch.setenv("TEDQ_GB300_NORMALISE", norm)
+    spec = _vqc_spec(14, 3, seed=21)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=jit, fuse=(norm != "f"))
+    if jit == 1:
+        assert cc._prog.jit_wait() is None
+    gen = torch.Generator().manual_seed(21)
+    # angles near 0, pi/2, pi and 3 pi / 2 select both normalised forms
+    params = (torch.randint(0, 4, (2, cc.num_params), generator=gen).double() * np.pi / 2
+              + 1e-3 * torch.randn(2, cc.num_params, generator=gen, dtype=torch.float64))
+    pd = params.to(DEV, torch.float32).requires_grad_(True)
+    out = cc.execute_batch(pd)
+    out.sum().backward()
+    for b in range(2):
+        want, want_g = oracle.value_and_grad(spec, params[b], np.ones(out.shape[1]), torch.complex128)
+        np.testing.assert_allclose(out[b].detach().cpu().double().numpy(), want.numpy(), atol=1e-5)
+        np.testing.assert_allclose(pd.grad[b].cpu().double().numpy(), want_g.numpy(), atol=5e-5, rtol=1e-4)

@@ -199,3 +199,22 @@ def test_staging_tables_match_tile_map(n, adjoint):
                 u = tid + k * T
                 assert (g_t | P["gk"][k]) == g_direct[u << e]
                 assert (s_t ^ P["sk"][k]) == plan_interp.swz_unit(u)
+
+
+@pytest.mark.parametrize("norm", ["0", "f", "b", "fbu"])
+def test_plan_register_gate_forms(monkeypatch, norm):
+    """Every choice of register-gate forms (TEDQ_GB300_NORMALISE) reproduces
+    the reference's outputs and gradients on the golden cases."""
+    monkeypatch.setenv("TEDQ_GB300_NORMALISE", norm)
+    for case in [c for c in CASES if c["params"]]:
+        cc = _compile(case, "c128", fuse=(norm != "f"))
+        fwd, bwd = cc.describe(), cc.describe(adjoint=True)
+        prm = np.asarray(case["params"], dtype=np.float64)
+        psi = plan_interp.forward(fwd, prm, _init(case))
+        got = _assemble(case, fwd, plan_interp.outputs(fwd, psi), psi)
+        if any(m["kind"] == "state" for m in case["meas"]):
+            continue
+        np.testing.assert_allclose(got, _arr(case["out_c128"]), atol=1e-12, rtol=1e-12)
+        dy = np.asarray(case["dy"], dtype=np.float64)
+        g = plan_interp.adjoint(bwd, prm, psi.copy(), dy[:fwd["n_real"]], None)
+        np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=1e-10, rtol=1e-9)
