@@ -108,6 +108,18 @@ struct TnDevice {
   void* g_out = nullptr;
   void* g_ws = nullptr;
   int64_t g_batch = -1;
+  // fused-step items of the level launches for batch `items_batch`
+  TnFusedItem* items = nullptr;
+  size_t items_cap = 0;
+  int64_t items_batch = -1;
+};
+
+// One level launch: the fused steps [step0, step1) of a network (same level).
+struct TnLevelRun {
+  int step0 = 0, step1 = 0;
+  int item0 = 0, n_items = 0;
+  int blocks = 0;
+  double flops = 0;
 };
 
 struct tedq_tn_plan {
@@ -120,6 +132,7 @@ struct tedq_tn_plan {
   int64_t const_total = 0, desc_total = 0;
   std::mutex mu;
   TnDevice dev[64];
+  std::vector<std::vector<TnLevelRun>> runs;  // per network, for the current item table
   // kernel timing (tedq_tn_profile_*)
   struct Ev {
     cudaEvent_t a, b;
@@ -221,6 +234,118 @@ int32_t ensure_device(tedq_tn_plan* p, int dev) {
   return TEDQ_OK;
 }
 
+// Item table of the level launches for `batch` (uploaded when the batch size
+// changes; offsets are relative to the workspace or the constants, so the
+// table does not depend on the buffers of a call).
+int32_t prepare_items(tedq_tn_plan* p, TnDevice& D, int64_t batch) {
+  if (D.items_batch == batch) return TEDQ_OK;
+  const Layout L = layout(p, batch);
+  const int64_t es = elem_bytes(p);
+  std::vector<TnFusedItem> items;
+  p->runs.assign(p->nets.size(), {});
+  for (size_t m = 0; m < p->nets.size(); ++m) {
+    const TnNet& net = p->nets[m];
+    const int64_t cb = p->const_base[m];
+    auto tensor_off = [&](const TnTensor& T, int& region) -> int64_t {
+      region = 0;
+      if (T.leaf >= 0) {
+        if (!T.batched) {
+          region = 1;
+          return cb + 2 * T.off;
+        }
+        return (int64_t)L.leaves / es + 2 * T.off * batch;
+      }
+      return T.batched ? (int64_t)L.arena_b / es + T.arena * batch : (int64_t)L.arena_u / es + T.arena;
+    };
+    size_t i = 0;
+    while (i < net.steps.size()) {
+      if (!net.steps[i].fused) {
+        ++i;
+        continue;
+      }
+      size_t j = i;
+      TnLevelRun run;
+      run.step0 = (int)i;
+      run.item0 = (int)items.size();
+      int64_t blocks = 0;
+      bool ok = true;
+      while (j < net.steps.size() && net.steps[j].fused && net.steps[j].level == net.steps[i].level) {
+        const TnStep& st = net.steps[j];
+        TnFusedItem it;
+        std::memset(&it, 0, sizeof(it));
+        it.lm = st.opa.nf;
+        it.ln = st.opb.nf;
+        it.lk = st.opa.nc;
+        it.nb = st.batched ? (int32_t)batch : 1;
+        ok &= it.lm <= kTnItemFree && it.ln <= kTnItemFree && it.lk <= kTnItemSum;
+        const TnOperand* ops[2] = {&st.opa, &st.opb};
+        for (int x = 0; x < 2 && ok; ++x) {
+          const TnOperand& op = *ops[x];
+          const TnTensor& T = net.tensors[op.tensor];
+          it.off[x] = tensor_off(T, it.region[x]);
+          const int64_t M = 1ll << T.lm, N = 1ll << T.ln, sj = T.split ? 2 * M : M;
+          it.bstride[x] = !T.batched ? 0 : (T.leaf >= 0 ? (2ll << T.full_idx.size()) : (2ll << (T.lm + T.ln)));
+          it.im[x] = T.leaf >= 0 ? 1 : (T.split ? M : M * N);
+          auto w = [&](int sbit) -> int64_t {
+            if (T.leaf >= 0) return 2ll << sbit;
+            return sbit < T.lm ? (1ll << sbit) : (sj << (sbit - T.lm));
+          };
+          if ((int)op.slice_bit.size() > kTnItemSlice) ok = false;
+          for (size_t q = 0; q < op.slice_bit.size() && ok; ++q) {
+            it.slq[x][q] = op.slice_bit[q].first;
+            it.slw[x][q] = (int32_t)w(op.slice_bit[q].second);
+          }
+          (x ? it.nsl1 : it.nsl0) = (int32_t)op.slice_bit.size();
+          for (int k = 0; k < op.nc && ok; ++k) it.wk[x][k] = (int32_t)w(op.src_bit[k]);
+          for (int k = 0; k < op.nf && ok; ++k) it.wf[x][k] = (int32_t)w(op.src_bit[op.nc + k]);
+        }
+        const TnTensor& O = net.tensors[st.out];
+        int reg = 0;
+        it.dst_off = tensor_off(O, reg);
+        it.dst_bstride = O.batched ? (2ll << (O.lm + O.ln)) : 0;
+        it.blk0 = (int32_t)blocks;
+        blocks += ((int64_t)it.nb << (it.lm + it.ln)) / 256 + ((((int64_t)it.nb << (it.lm + it.ln)) % 256) ? 1 : 0);
+        run.flops += 8.0 * std::ldexp(1.0, it.lm + it.ln + it.lk) * (double)it.nb;
+        items.push_back(it);
+        ++j;
+      }
+      if (!ok || blocks > 0x7fffffffll) {
+        // outside the item limits: these steps run one launch each
+        items.resize(run.item0);
+        for (size_t k = i; k < j; ++k) {
+          TnLevelRun one;
+          one.step0 = (int)k;
+          one.step1 = (int)k + 1;
+          one.n_items = 0;
+          p->runs[m].push_back(one);
+        }
+      } else {
+        run.step1 = (int)j;
+        run.n_items = (int)(j - i);
+        run.blocks = (int)blocks;
+        p->runs[m].push_back(run);
+      }
+      i = j;
+    }
+  }
+  const size_t bytes = std::max<size_t>(items.size(), 1) * sizeof(TnFusedItem);
+  if (bytes > D.items_cap) {
+    if (D.items) cudaFree(D.items);
+    D.items = nullptr;
+    D.items_cap = 0;
+    TEDQ_CUDA("tedq_tn_contract: cudaMalloc", cudaMalloc(&D.items, bytes));
+    D.items_cap = bytes;
+  }
+  if (!items.empty()) {
+    // launches of earlier calls may still read the previous table
+    TEDQ_CUDA("tedq_tn_contract: cudaDeviceSynchronize", cudaDeviceSynchronize());
+    TEDQ_CUDA("tedq_tn_contract: cudaMemcpy",
+              cudaMemcpy(D.items, items.data(), items.size() * sizeof(TnFusedItem), cudaMemcpyHostToDevice));
+  }
+  D.items_batch = batch;
+  return TEDQ_OK;
+}
+
 // Runs one launch; with profiling on, brackets it with events on its stream.
 template <typename F>
 int32_t timed(tedq_tn_plan* p, cudaStream_t s, int family, double work, F&& launch) {
@@ -318,9 +443,24 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       for (int j = 0; j < op.nf; ++j) o.wf[j] = w(op.src_bit[op.nc + j]);
     };
     const int64_t n_slices = 1ll << net.sliced.size();
+    const std::vector<TnLevelRun>& runs = p->runs[m];
     for (int64_t sl = 0; sl < n_slices; ++sl) {
-      for (const TnStep& stp : net.steps) {
+      size_t next_run = 0;
+      for (size_t si = 0; si < net.steps.size(); ++si) {
+        const TnStep& stp = net.steps[si];
+        if (stp.fused && next_run < runs.size() && runs[next_run].step0 == (int)si && runs[next_run].n_items > 0) {
+          const TnLevelRun& run = runs[next_run++];
+          int32_t rc = timed(p, s, 2, run.flops, [&]() -> int32_t {
+            TEDQ_CUDA("tedq_tn_contract: fused level kernel",
+                      tn_fused_level<real>(D.items + run.item0, run.n_items, run.blocks, ws, D.consts, sl, s));
+            return TEDQ_OK;
+          });
+          if (rc != TEDQ_OK) return rc;
+          si = run.step1 - 1;
+          continue;
+        }
         if (stp.fused) {
+          if (next_run < runs.size() && runs[next_run].step0 == (int)si) ++next_run;
           const TnTensor& T = net.tensors[stp.out];
           TnFusedArgs F;
           std::memset(&F, 0, sizeof(F));
@@ -409,6 +549,8 @@ int32_t contract(tedq_tn_plan* p, TnDevice& D, const void* params, int64_t batch
                  cudaStream_t s) {
   const real* prm = static_cast<const real*>(params);
   real* o = static_cast<real*>(out);
+  const int32_t prc = prepare_items(p, D, batch);
+  if (prc != TEDQ_OK) return prc;
   if (!p->graphs || p->profiling) return enqueue<real>(p, D, prm, batch, o, ws, s);
   const bool same = D.g_params == params && D.g_out == out && D.g_ws == ws && D.g_batch == batch;
   if (!same) {
@@ -448,12 +590,13 @@ void release_devices(tedq_tn_plan* p) {
   cudaGetDevice(&cur);
   for (int d = 0; d < 64; ++d) {
     TnDevice& D = p->dev[d];
-    if (!D.handle && !D.consts && !D.desc && !D.exec && !D.capture) continue;
+    if (!D.handle && !D.consts && !D.desc && !D.exec && !D.capture && !D.items) continue;
     cudaSetDevice(d);
     if (D.exec) cudaGraphExecDestroy(D.exec);
     if (D.capture) cudaStreamDestroy(D.capture);
     if (D.consts) cudaFree(D.consts);
     if (D.desc) cudaFree(D.desc);
+    if (D.items) cudaFree(D.items);
     if (D.handle) blas().destroy(D.handle);
     D = TnDevice();
   }
@@ -486,7 +629,9 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
       if (opts->repeats > 0) po.repeats = opts->repeats;
       if (opts->seed) po.seed = opts->seed;
     }
-    if (const char* env = getenv("TEDQ_GB300_TN_FUSED_LOG2")) po.fused_log2 = atoi(env);  // tuning
+    // tuning; at most 13 keeps every fused operand within the level-launch
+    // item limits (12 free, 8 contracted bits)
+    if (const char* env = getenv("TEDQ_GB300_TN_FUSED_LOG2")) po.fused_log2 = std::max(0, std::min(13, atoi(env)));
     p->n = n_qubits;
     for (int i = 0; i < n_gates && gates; ++i)
       for (int j = 0; j < 3; ++j) p->n_params = std::max(p->n_params, gates[i].param_slot[j] + 1);

@@ -176,6 +176,63 @@ __global__ void __launch_bounds__(256) tn_fused_kernel(const __grid_constant__ T
   }
 }
 
+// One CTA = 256 outputs of one item; the item is found by binary search on
+// blk0.  Contracted-index offsets of both operands are tabulated in shared
+// memory first (every thread reaches the barrier before any exits).
+template <typename real>
+__global__ void __launch_bounds__(256) tn_fused_level_kernel(const TnFusedItem* __restrict__ items, int n_items,
+                                                             char* __restrict__ ws, const char* __restrict__ consts,
+                                                             int64_t slice) {
+  __shared__ int32_t koff[2][256];
+  int lo = 0, hi = n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (items[mid].blk0 <= (int)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const TnFusedItem& it = items[lo];
+  const int lk = it.lk, K = 1 << lk;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    int32_t oa = 0, ob = 0;
+    for (int j = 0; j < lk; ++j)
+      if ((k >> j) & 1) {
+        oa += it.wk[0][j];
+        ob += it.wk[1][j];
+      }
+    koff[0][k] = oa;
+    koff[1][k] = ob;
+  }
+  __syncthreads();
+  const int lm = it.lm, lmn = lm + it.ln;
+  const int64_t MN = 1ll << lmn, total = MN * it.nb;
+  const int64_t t = (int64_t)(blockIdx.x - it.blk0) * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int64_t b = t >> lmn, idx = t & (MN - 1);
+  const int64_t i = idx & ((1ll << lm) - 1), j = idx >> lm;
+  int64_t oa = it.off[0] + b * it.bstride[0], ob = it.off[1] + b * it.bstride[1];
+  for (int q = 0; q < it.nsl0; ++q)
+    if ((slice >> it.slq[0][q]) & 1) oa += it.slw[0][q];
+  for (int q = 0; q < it.nsl1; ++q)
+    if ((slice >> it.slq[1][q]) & 1) ob += it.slw[1][q];
+  for (int q = 0; q < lm; ++q)
+    if ((i >> q) & 1) oa += it.wf[0][q];
+  for (int q = 0; q < it.ln; ++q)
+    if ((j >> q) & 1) ob += it.wf[1][q];
+  const real* pa = reinterpret_cast<const real*>(it.region[0] ? consts : ws) + oa;
+  const real* pb = reinterpret_cast<const real*>(it.region[1] ? consts : ws) + ob;
+  const int64_t ima = it.im[0], imb = it.im[1];
+  real re = 0, im = 0;
+  for (int k = 0; k < K; ++k) {
+    const real ar = pa[koff[0][k]], ai = pa[koff[0][k] + ima];
+    const real br = pb[koff[1][k]], bi = pb[koff[1][k] + imb];
+    re = fma(ar, br, fma(-ai, bi, re));
+    im = fma(ar, bi, fma(ai, br, im));
+  }
+  real* d = reinterpret_cast<real*>(ws) + it.dst_off + b * it.dst_bstride;
+  d[idx] = re;
+  d[MN + idx] = im;
+}
+
 template <typename real>
 __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
                                real* out, int n_meas, int m, int first, int last) {
@@ -223,6 +280,14 @@ cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream) {
 }
 
 template <typename real>
+cudaError_t tn_fused_level(const TnFusedItem* items, int n_items, int blocks, char* ws, const void* consts,
+                           int64_t slice, cudaStream_t stream) {
+  if (n_items <= 0 || blocks <= 0) return cudaErrorInvalidValue;
+  return launch_kernel(tn_fused_level_kernel<real>, dim3((unsigned)blocks), dim3(256), 0, stream, items, n_items, ws,
+                       static_cast<const char*>(consts), slice);
+}
+
+template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
                     int m, int first, int last, cudaStream_t stream) {
   const unsigned blocks = (unsigned)((batch + 255) / 256);
@@ -237,6 +302,9 @@ template cudaError_t tn_gather<float>(const TnGatherArgs&, cudaStream_t);
 template cudaError_t tn_gather<double>(const TnGatherArgs&, cudaStream_t);
 template cudaError_t tn_fused<float>(const TnFusedArgs&, cudaStream_t);
 template cudaError_t tn_fused<double>(const TnFusedArgs&, cudaStream_t);
+template cudaError_t tn_fused_level<float>(const TnFusedItem*, int, int, char*, const void*, int64_t, cudaStream_t);
+template cudaError_t tn_fused_level<double>(const TnFusedItem*, int, int, char*, const void*, int64_t,
+                                            cudaStream_t);
 template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int, cudaStream_t);
 template cudaError_t tn_root<double>(const double*, int64_t, int64_t, double*, double*, int, int, int, int,
                                      cudaStream_t);

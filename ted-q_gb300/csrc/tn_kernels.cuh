@@ -72,6 +72,35 @@ struct TnFusedArgs {
 template <typename real>
 cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream);
 
+// One fused contraction of a level launch (all fused steps of one dependency
+// level run in one kernel).  Offsets are in reals from a region base (0: the
+// call's workspace, 1: the plan's constant leaves), so one table serves every
+// call with the same batch size.  Operand element (f, k) has its real part at
+// base + b * bstride + sum_j bit_j(f) wf[j] + sum_j bit_j(k) wk[j] (+ the
+// slice weights of the sliced indices set in the current slice) and its
+// imaginary part `im` reals further; the result is planar (Re at j * M + i,
+// Im at + M * N).
+constexpr int kTnItemFree = 12, kTnItemSum = 8, kTnItemSlice = 6;
+struct TnFusedItem {
+  int64_t off[2];      // operand a / b
+  int64_t bstride[2];  // 0: shared by all circuits
+  int64_t im[2];
+  int64_t dst_off, dst_bstride;
+  int32_t region[2];
+  int32_t nb;    // circuits computed (1: unbatched step)
+  int32_t blk0;  // first CTA of the item within its level launch
+  int32_t lm, ln, lk, nsl0, nsl1, pad;
+  int32_t slq[2][kTnItemSlice];  // sliced index numbers
+  int32_t slw[2][kTnItemSlice];  // their weights (reals)
+  int32_t wf[2][kTnItemFree];
+  int32_t wk[2][kTnItemSum];
+};
+
+// Items [0, n_items) of one level; grid = blk0 of the last item + its CTAs.
+template <typename real>
+cudaError_t tn_fused_level(const TnFusedItem* items, int n_items, int blocks, char* ws, const void* consts,
+                           int64_t slice, cudaStream_t stream);
+
 template <typename real>
 cudaError_t tn_build_leaves(const TnLeafDesc* desc, int n_desc, const real* params, int n_params, int64_t batch,
                             real* leaves, cudaStream_t stream);

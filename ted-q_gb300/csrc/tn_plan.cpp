@@ -515,6 +515,7 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
 
   // steps, gather tables and liveness-planned arenas
   Arena ab, au;  // batched (reals per batch entry) / unbatched (reals)
+  std::map<int, int> producer;  // intermediate tensor -> step
   for (auto& pr : best.pairs) {
     TnStep st;
     st.a = pr.first;
@@ -562,17 +563,10 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
       st.fused = lm + ln + lk < opt.fused_log2 && lk <= 8 && (lm + ln >= 5 || lk <= 6);
       if (st.fused) st.double_a = false;
     }
-    // a gathered step copies its inputs to the operand scratch before the
-    // GEMM writes, so its output may reuse their space; a fused step reads
-    // its inputs while it writes, so its output is placed first
-    auto release_inputs = [&]() {
-      for (int t : {st.a, st.b}) {
-        const TnTensor& T = net.tensors[t];
-        if (T.leaf >= 0) continue;
-        (T.batched ? ab : au).release(T.arena, inter_reals(T));
-      }
-    };
-    if (!st.fused) release_inputs();
+    int lv = 0;
+    for (int t : {st.a, st.b})
+      if (net.tensors[t].leaf < 0) lv = std::max(lv, net.steps[producer[t]].level + 1);
+    st.level = lv;
     TnTensor out;
     out.idx = st.free_b;
     out.idx.insert(out.idx.end(), st.free_a.begin(), st.free_a.end());
@@ -580,14 +574,45 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
     out.ln = (int)st.free_b.size();
     out.split = st.double_a;
     out.batched = st.batched;
-    out.arena = (out.batched ? ab : au).alloc(inter_reals(out));
-    if (st.fused) release_inputs();
     st.out = (int)net.tensors.size();
     net.tensors.push_back(out);
+    producer[st.out] = (int)net.steps.size();
     net.steps.push_back(std::move(st));
   }
   if (net.steps.empty()) throw std::logic_error("empty contraction");
   net.root = net.steps.back().out;
+  // execution order: by level, a level's fused steps (one launch) first
+  std::stable_sort(net.steps.begin(), net.steps.end(), [](const TnStep& x, const TnStep& y) {
+    return x.level != y.level ? x.level < y.level : (x.fused && !y.fused);
+  });
+  // Liveness-planned arenas in that order.  The fused steps of a level run
+  // concurrently and read their inputs in place: all their outputs are placed
+  // before any of their inputs is released.  A gathered step copies its
+  // inputs to the operand scratch before the GEMM writes, so its output may
+  // reuse their space.
+  auto release_inputs = [&](const TnStep& st) {
+    for (int t : {st.a, st.b}) {
+      const TnTensor& T = net.tensors[t];
+      if (T.leaf >= 0) continue;
+      (T.batched ? ab : au).release(T.arena, inter_reals(T));
+    }
+  };
+  auto place = [&](const TnStep& st) {
+    TnTensor& T = net.tensors[st.out];
+    T.arena = (T.batched ? ab : au).alloc(inter_reals(T));
+  };
+  for (size_t i = 0; i < net.steps.size();) {
+    size_t j = i;
+    while (j < net.steps.size() && net.steps[j].fused && net.steps[j].level == net.steps[i].level) ++j;
+    for (size_t k = i; k < j; ++k) place(net.steps[k]);
+    for (size_t k = i; k < j; ++k) release_inputs(net.steps[k]);
+    if (j == i) {
+      release_inputs(net.steps[i]);
+      place(net.steps[i]);
+      j = i + 1;
+    }
+    i = j;
+  }
   if (!net.tensors[net.root].idx.empty()) throw std::logic_error("open indices at the root");
   net.batched_arena = ab.top;
   net.unbatched_arena = au.top;
@@ -664,7 +689,7 @@ std::string tn_describe(const std::vector<TnNet>& nets, int n_params, int precis
       const TnStep& s = n.steps[i];
       o << (i ? "," : "") << "{\"a\":" << s.a << ",\"b\":" << s.b << ",\"out\":" << s.out
         << ",\"batched\":" << (s.batched ? 1 : 0) << ",\"double_a\":" << (s.double_a ? 1 : 0)
-        << ",\"fused\":" << (s.fused ? 1 : 0) << ",\"opa\":";
+        << ",\"fused\":" << (s.fused ? 1 : 0) << ",\"level\":" << s.level << ",\"opa\":";
       operand_json(o, s.opa);
       o << ",\"opb\":";
       operand_json(o, s.opb);

@@ -87,6 +87,10 @@ struct TnStep {
   // small contraction: one fused kernel reads both operands in place and
   // writes the planar result (no gathers, no GEMM call)
   bool fused = false;
+  // dependency depth (leaf inputs only: 0).  Steps are stored by level, the
+  // fused ones of a level first: one launch runs all fused steps of a level
+  // together, then the level's GEMM steps run one by one.
+  int level = 0;
 };
 
 struct TnNet {

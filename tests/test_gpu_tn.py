@@ -132,3 +132,18 @@ def test_tn_workspace_and_errors():
     P = torch.zeros((1, prog.n_params + 1), device=DEV)
     with pytest.raises(ValueError):
         cc.execute_batch(P)
+
+
+def test_tn_level_launch_tables_follow_batch_size():
+    """The item tables of the level launches (all fused steps of one
+    dependency level in one kernel) are rebuilt when the batch size changes:
+    calls alternating between batch sizes agree with one-circuit calls."""
+    spec = hea_spec(10, 3)
+    cc = _tn(spec, "c64", "fp32", requires_grad=False)
+    n = len(flat_params(spec))
+    gen = torch.Generator().manual_seed(4)
+    P = (torch.rand(7, n, generator=gen) * 6.28).to(DEV)
+    ones = torch.cat([cc.execute_batch(P[i:i + 1]) for i in range(7)])
+    for rows in (3, 7, 3, 5):
+        got = cc.execute_batch(P[:rows])
+        torch.testing.assert_close(got, ones[:rows], atol=2e-6, rtol=1e-5)

@@ -108,18 +108,26 @@ def run(desc, prm):
 
 
 def check_arenas(net):
-    """Live intermediates never overlap in their arena (batched and unbatched
-    separately); the output of a gathered step may reuse the space of its
-    inputs, the output of a fused step (which reads its inputs in place) not."""
+    """Steps run by level (inputs from lower levels only), a level's fused
+    steps first and together.  Live intermediates never overlap in their
+    arena (batched and unbatched separately); the output of a gathered step
+    may reuse the space of its inputs, the outputs of a level's fused steps
+    (which read their inputs in place, concurrently) overlap no input of the
+    level and no other output."""
     T = net["tensors"]
     L = net["n_leaves"]
+    steps = net["steps"]
+    level_of = {}
+    for st in steps:
+        for t in (st["a"], st["b"]):
+            if t >= L:
+                assert level_of[t] < st["level"], "input from the same or a later level"
+        level_of[st["out"]] = st["level"]
+    keys = [(st["level"], 0 if st["fused"] else 1) for st in steps]
+    assert keys == sorted(keys), "steps not ordered by level, fused first"
     live = {}
-    for st in net["steps"]:
-        if not st["fused"]:
-            for t in (st["a"], st["b"]):
-                if t >= L:
-                    live.pop(t)
-        o = st["out"]
+
+    def place(o):
         size = 2 << (T[o]["lm"] + T[o]["ln"])
         lo, hi = T[o]["arena"], T[o]["arena"] + size
         arena_max = net["batched_arena"] if T[o]["batched"] else net["unbatched_arena"]
@@ -127,9 +135,26 @@ def check_arenas(net):
         for t, (b, l2, h2) in live.items():
             if b == T[o]["batched"]:
                 assert hi <= l2 or h2 <= lo, f"tensor {o} overlaps live tensor {t}"
-        if st["fused"]:
+        live[o] = (T[o]["batched"], lo, hi)
+
+    i = 0
+    while i < len(steps):
+        j = i
+        while j < len(steps) and steps[j]["fused"] and steps[j]["level"] == steps[i]["level"]:
+            j += 1
+        if j > i:
+            for st in steps[i:j]:
+                place(st["out"])
+            for st in steps[i:j]:
+                for t in (st["a"], st["b"]):
+                    if t >= L:
+                        live.pop(t)
+        else:
+            st = steps[i]
             for t in (st["a"], st["b"]):
                 if t >= L:
                     live.pop(t)
-        live[o] = (T[o]["batched"], lo, hi)
+            place(st["out"])
+            j = i + 1
+        i = j
     assert list(live) == [net["root"]]
