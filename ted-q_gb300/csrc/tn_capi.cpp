@@ -402,22 +402,49 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       });
       if (rc != TEDQ_OK) return rc;
     }
-    auto source = [&](int t, TnGatherOp& o) {
-      const TnTensor& T = net.tensors[t];
+    // gather operand: source weights of the element bits, slice offset and
+    // the copy tiles (lowest source offsets and lowest element bits)
+    auto gather_op = [&](const TnOperand& op, int64_t sl, TnGatherOp& o) {
+      const TnTensor& T = net.tensors[op.tensor];
+      std::memset(&o, 0, sizeof(o));
+      o.nbits = op.nf + op.nc;
+      const int64_t M = 1ll << T.lm, N = 1ll << T.ln, sj = T.split ? 2 * M : M;
+      auto w = [&](int sbit) -> int64_t {
+        if (T.leaf >= 0) return 2ll << sbit;
+        return sbit < T.lm ? (1ll << sbit) : (sj << (sbit - T.lm));
+      };
       if (T.leaf >= 0) {
-        o.kind = 0;
-        o.lm = 0;
         o.src = T.batched ? leaves + 2 * T.off * batch : consts + 2 * T.off;
         o.src_bstride = T.batched ? (2ll << T.full_idx.size()) : 0;
+        o.src_im = 1;
+        for (auto& qb : op.slice_bit) o.src_base += ((sl >> qb.first) & 1) ? w(qb.second) : 0;
       } else {
-        o.kind = 1;
-        o.lm = T.lm;
-        const int64_t M = 1ll << T.lm, N = 1ll << T.ln;
-        o.sj = T.split ? 2 * M : M;
-        o.sp = T.split ? M : M * N;
         o.src = T.batched ? arena_b + T.arena * batch : arena_u + T.arena;
         o.src_bstride = T.batched ? (2ll << (T.lm + T.ln)) : 0;
+        o.src_im = T.split ? M : M * N;
       }
+      for (int j = 0; j < o.nbits; ++j) o.sw[j] = w(op.src_bit[j]);
+      o.nb = T.batched ? batch : 1;
+      o.nc = op.nc;
+      o.doubled = op.doubled ? 1 : 0;
+      std::vector<int> by_src(o.nbits);
+      for (int j = 0; j < o.nbits; ++j) by_src[j] = j;
+      std::sort(by_src.begin(), by_src.end(), [&](int x, int y) { return o.sw[x] < o.sw[y]; });
+      const int nlow = std::min(5, o.nbits);
+      std::vector<int> tile, rd;
+      for (int j = 0; j < nlow; ++j) tile.push_back(j);                       // written in order
+      for (int q = 0; q < nlow; ++q)
+        if (by_src[q] >= nlow) tile.push_back(by_src[q]);                     // read in order
+      for (int q = 0; q < nlow; ++q) rd.push_back(by_src[q]);
+      for (int j = 0; j < nlow; ++j)
+        if (std::find(rd.begin(), rd.end(), j) == rd.end()) rd.push_back(j);
+      o.tb = (int32_t)tile.size();
+      for (int i = 0; i < o.tb; ++i) {
+        o.tile_bit[i] = (int8_t)tile[i];
+        o.r2w[i] = (int8_t)(std::find(tile.begin(), tile.end(), rd[i]) - tile.begin());
+      }
+      for (int j = 0; j < o.nbits; ++j)
+        if (std::find(tile.begin(), tile.end(), j) == tile.end()) o.outer_bit[o.n_outer++] = (int8_t)j;
     };
     // fused operand: per-bit offsets (reals) of the source storage
     auto fused_op = [&](const TnOperand& op, int64_t sl, TnFusedOp& o) {
@@ -486,17 +513,9 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         std::memset(&A, 0, sizeof(A));
         const TnOperand* ops[2] = {&stp.opa, &stp.opb};
         for (int x = 0; x < 2; ++x) {
-          const TnOperand& op = *ops[x];
-          TnGatherOp& o = A.op[x];
-          source(op.tensor, o);
-          o.nbits = op.nf + op.nc;
-          if (o.nbits > kTnMaxBits) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
-          for (int j = 0; j < o.nbits; ++j) o.bit[j] = (int8_t)op.src_bit[j];
-          o.base = 0;
-          for (auto& qb : op.slice_bit) o.base += ((sl >> qb.first) & 1) << qb.second;
-          o.nb = net.tensors[op.tensor].batched ? batch : 1;
-          o.nc = op.nc;
-          o.doubled = op.doubled ? 1 : 0;
+          if (ops[x]->nf + ops[x]->nc > kTnMaxBits)
+            return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
+          gather_op(*ops[x], sl, A.op[x]);
         }
         A.op[0].dst = scratch;
         A.op[1].dst = scratch + ((A.op[0].doubled ? 4ll : 2ll) << A.op[0].nbits) * A.op[0].nb;

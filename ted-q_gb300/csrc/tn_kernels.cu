@@ -96,38 +96,84 @@ __global__ void __launch_bounds__(256) tn_leaf_kernel(const TnLeafDesc* __restri
   }
 }
 
+// Tiled bit-permutation copy (one operand per blockIdx.y): per tile, source
+// elements are read in source order into shared memory (padded one word per
+// 32) and written out in destination order, so both sides are coalesced.
+// Offsets of the tile-local and of the low 8 outer element bits are tabulated
+// once per CTA.
 template <typename real>
 __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ TnGatherArgs A) {
+  constexpr int TS_MAX = 1 << kTnTileBits;
+  __shared__ real sre[TS_MAX + TS_MAX / 32], sim[TS_MAX + TS_MAX / 32];
+  __shared__ int64_t stab[TS_MAX], dtab[TS_MAX];
+  __shared__ int64_t olo_s[256], olo_d[256];
+  __shared__ int16_t r2w_tab[TS_MAX];
   const TnGatherOp& o = A.op[blockIdx.y];
-  const int nbits = o.nbits;
-  const int64_t n = 1ll << nbits, total = n * o.nb;
-  const int64_t K = 1ll << o.nc, imask = (1ll << o.lm) - 1;
+  const int tb = o.tb, TS = 1 << tb, nc = o.nc;
+  const int64_t K = 1ll << nc, n = 1ll << o.nbits;
+  auto dw = [&](int j) -> int64_t { return j < nc ? (1ll << j) : ((2 * K) << (j - nc)); };
+  for (int w = threadIdx.x; w < TS; w += blockDim.x) {
+    int64_t so = 0, dof = 0;
+    int rw = 0;
+    for (int i = 0; i < tb; ++i)
+      if ((w >> i) & 1) {
+        const int j = o.tile_bit[i];
+        so += o.sw[j];
+        dof += dw(j);
+        rw |= 1 << o.r2w[i];
+      }
+    stab[w] = so;
+    dtab[w] = dof;
+    r2w_tab[w] = (int16_t)rw;
+  }
+  const int nlo = o.n_outer < 8 ? o.n_outer : 8;
+  for (int u = threadIdx.x; u < (1 << nlo); u += blockDim.x) {
+    int64_t so = 0, dof = 0;
+    for (int q = 0; q < nlo; ++q)
+      if ((u >> q) & 1) {
+        so += o.sw[o.outer_bit[q]];
+        dof += dw(o.outer_bit[q]);
+      }
+    olo_s[u] = so;
+    olo_d[u] = dof;
+  }
+  __syncthreads();
+  const int outer = o.nbits - tb;
+  const int64_t total = o.nb << outer;
   const int64_t dstride = (o.doubled ? 4 : 2) * n;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = t >> nbits, e = t & (n - 1);
-    int64_t flat = o.base;
-    for (int j = 0; j < nbits; ++j) flat += ((e >> j) & 1) << o.bit[j];
-    const real* s = static_cast<const real*>(o.src) + b * o.src_bstride;
-    real re, im;
-    if (o.kind == 0) {
-      re = s[2 * flat];
-      im = s[2 * flat + 1];
-    } else {
-      const int64_t at = (flat >> o.lm) * o.sj + (flat & imask);
-      re = s[at];
-      im = s[at + o.sp];
+  const real* src = static_cast<const real*>(o.src);
+  real* dst = static_cast<real*>(o.dst);
+  for (int64_t tile = blockIdx.x; tile < total; tile += gridDim.x) {
+    const int64_t b = tile >> outer, ou = tile & ((1ll << outer) - 1);
+    int64_t so = o.src_base + b * o.src_bstride + olo_s[ou & ((1 << nlo) - 1)];
+    int64_t dof = b * dstride + olo_d[ou & ((1 << nlo) - 1)];
+    for (int q = nlo; q < o.n_outer; ++q)
+      if ((ou >> q) & 1) {
+        so += o.sw[o.outer_bit[q]];
+        dof += dw(o.outer_bit[q]);
+      }
+    const real* s = src + so;
+    for (int r = threadIdx.x; r < TS; r += blockDim.x) {
+      const int w = r2w_tab[r];
+      const int64_t at = stab[w];
+      sre[w + (w >> 5)] = s[at];
+      sim[w + (w >> 5)] = s[at + o.src_im];
     }
-    real* d = static_cast<real*>(o.dst) + b * dstride;
-    const int64_t f = e >> o.nc, k = e & (K - 1);
-    real* row = d + f * 2 * K + k;
-    row[0] = re;
-    if (!o.doubled) {
-      row[K] = im;
-    } else {
-      row[K] = -im;
-      row[n * 2] = im;  // row F + f
-      row[n * 2 + K] = re;
+    __syncthreads();
+    real* d = dst + dof;
+    for (int w = threadIdx.x; w < TS; w += blockDim.x) {
+      const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
+      real* row = d + dtab[w];
+      row[0] = re;
+      if (!o.doubled) {
+        row[K] = im;
+      } else {
+        row[K] = -im;
+        row[n * 2] = im;  // row F + f
+        row[n * 2 + K] = re;
+      }
     }
+    __syncthreads();
   }
 }
 
@@ -262,11 +308,13 @@ template <typename real>
 cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
   int64_t most = 0;
   for (int i = 0; i < 2; ++i) {
-    const int64_t t = (1ll << args.op[i].nbits) * args.op[i].nb;
+    const TnGatherOp& o = args.op[i];
+    if (o.tb < 0 || o.tb > kTnTileBits || o.tb > o.nbits || o.n_outer != o.nbits - o.tb) return cudaErrorInvalidValue;
+    const int64_t t = o.nb << (o.nbits - o.tb);
     most = t > most ? t : most;
   }
-  int64_t blocks = (most + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  int64_t blocks = most;
+  if (blocks > 152 * 8) blocks = 152 * 8;
   return launch_kernel(tn_gather_kernel<real>, dim3((unsigned)blocks, 2), dim3(256), 0, stream, args);
 }
 

@@ -24,22 +24,28 @@ struct TnLeafDesc {
 constexpr int kTnMaxBits = 48;
 
 // One GEMM operand: element e = f*K + k of the gather (n = F*K entries, nbits =
-// log2 n, K = 2^nc) takes source flat index base + sum_j bit_j(e) << bit[j].
+// log2 n, K = 2^nc) has its real part at source offset src_base +
+// sum_j bit_j(e) * sw[j] (reals) and its imaginary part src_im reals further.
 // Output rows of 2K reals: row f = [Re(f, 0..K), Im(f, 0..K)]; a doubled
 // operand writes [Re, -Im] in row f and [Im, Re] in row F + f.
+// The copy runs in tiles of 2^tb elements staged in shared memory: the tile
+// holds the element bits of the lowest source offsets (read in order) and the
+// 5 lowest element bits (written in order).  tile_bit lists the tile's element
+// bits in write order; r2w maps read-order tile bit i to its write-order bit;
+// outer_bit lists the remaining element bits.
+constexpr int kTnTileBits = 10;
 struct TnGatherOp {
   const void* src;
   void* dst;
   int64_t src_bstride;  // reals between batch entries of the source (0: shared)
-  int64_t base;         // flat-index offset of the current slice
+  int64_t src_base;     // reals: slice offset
+  int64_t src_im;       // reals from the real to the imaginary part
   int64_t nb;           // batch entries gathered (1 for a shared operand)
-  int64_t sj, sp;       // intermediate source: Re(i, j) at j*sj + i, Im at + sp
-  int32_t kind;         // 0: interleaved complex leaf, 1: intermediate
-  int32_t lm;           // intermediate source: log2 of its i extent
-  int32_t nbits, nc;
-  int32_t doubled;
-  int32_t pad;
-  int8_t bit[kTnMaxBits];
+  int64_t sw[kTnMaxBits];
+  int32_t nbits, nc, doubled, tb, n_outer, pad;
+  int8_t tile_bit[kTnTileBits];
+  int8_t r2w[kTnTileBits];
+  int8_t outer_bit[kTnMaxBits];
 };
 
 struct TnGatherArgs {
