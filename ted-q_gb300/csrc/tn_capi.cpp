@@ -45,6 +45,8 @@ struct Blas {
   cublasStatus_t (*set_stream)(cublasHandle_t, cudaStream_t) = nullptr;
   cublasStatus_t (*set_workspace)(cublasHandle_t, void*, size_t) = nullptr;
   cublasStatus_t (*set_emulation)(cublasHandle_t, cublasEmulationStrategy_t) = nullptr;
+  // optional: special-value handling of emulated GEMMs
+  cublasStatus_t (*set_special)(cublasHandle_t, cudaEmulationSpecialValuesSupport) = nullptr;
   const char* (*status_string)(cublasStatus_t) = nullptr;
   cublasStatus_t (*gemm)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int, int, int, const void*,
                          const void*, cudaDataType, int, long long, const void*, cudaDataType, int, long long,
@@ -79,6 +81,7 @@ Blas load_blas() {
   TEDQ_SYM(status_string, "cublasGetStatusString")
   TEDQ_SYM(gemm, "cublasGemmStridedBatchedEx")
 #undef TEDQ_SYM
+  b.set_special = reinterpret_cast<decltype(b.set_special)>(dlsym(h, "cublasSetEmulationSpecialValuesSupport"));
   b.ok = true;
   return b;
 }
@@ -207,6 +210,15 @@ int32_t ensure_device(tedq_tn_plan* p, int dev) {
     if (p->precision == TEDQ_PREC_C64 && (p->gemm == TEDQ_TN_GEMM_BF16X9 || p->gemm == TEDQ_TN_GEMM_AUTO)) {
       st = B.set_emulation(D.handle, CUBLAS_EMULATION_STRATEGY_EAGER);
       if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetEmulationStrategy", st);
+      // operands are finite whenever the parameters are (gate entries and
+      // their products): no scan and patch passes for infinities and NaNs.
+      // Circuits with a non-finite parameter are flagged by the gate-tensor
+      // kernel and return NaN from the root kernel instead.
+      if (B.set_special) {
+        st = B.set_special(D.handle, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE);
+        if (st != CUBLAS_STATUS_SUCCESS)
+          return blas_fail("tedq_tn_contract: cublasSetEmulationSpecialValuesSupport", st);
+      }
     }
   }
   const size_t es = (size_t)elem_bytes(p);
@@ -554,7 +566,8 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       const real* root = R.batched ? arena_b + R.arena * batch : arena_u + R.arena;
       int32_t rc = timed(p, s, 3, 0.0, [&]() -> int32_t {
         TEDQ_CUDA("tedq_tn_contract: root kernel",
-                  tn_root<real>(root, R.batched ? 2 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1, s));
+                  tn_root<real>(root, R.batched ? 2 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1,
+                                params, p->n_params, s));
         return TEDQ_OK;
       });
       if (rc != TEDQ_OK) return rc;

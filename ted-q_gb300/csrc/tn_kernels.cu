@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) tn_leaf_kernel(const TnLeafDesc* __restri
   }
 }
 
-// Tiled bit-permutation copy (one operand per blockIdx.y): per tile, source
+// Tiled bit-permutation copy (one operand per blockIdx.y, 256 threads): per tile, source
 // elements are read in source order into shared memory (padded one word per
 // 32) and written out in destination order, so both sides are coalesced.
 // Offsets of the tile-local and of the low 8 outer element bits are tabulated
@@ -153,11 +153,28 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
         dof += dw(o.outer_bit[q]);
       }
     const real* s = src + so;
-    for (int r = threadIdx.x; r < TS; r += blockDim.x) {
-      const int w = r2w_tab[r];
-      const int64_t at = stab[w];
-      sre[w + (w >> 5)] = s[at];
-      sim[w + (w >> 5)] = s[at + o.src_im];
+    // all loads of the tile first (up to 4 per thread), then the stores to
+    // shared memory: the loads are in flight together
+    constexpr int PER = TS_MAX / 256;
+    real vr[PER], vi[PER];
+    int wv[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int r = threadIdx.x + q * 256;
+      wv[q] = r < TS ? r2w_tab[r] : 0;
+      if (r < TS) {
+        const int64_t at = stab[wv[q]];
+        vr[q] = s[at];
+        vi[q] = s[at + o.src_im];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int w = wv[q];
+      if (threadIdx.x + q * 256 < TS) {
+        sre[w + (w >> 5)] = vr[q];
+        sim[w + (w >> 5)] = vi[q];
+      }
     }
     __syncthreads();
     real* d = dst + dof;
@@ -268,6 +285,7 @@ __global__ void __launch_bounds__(256) tn_fused_level_kernel(const TnFusedItem* 
   const real* pb = reinterpret_cast<const real*>(it.region[1] ? consts : ws) + ob;
   const int64_t ima = it.im[0], imb = it.im[1];
   real re = 0, im = 0;
+#pragma unroll 4
   for (int k = 0; k < K; ++k) {
     const real ar = pa[koff[0][k]], ai = pa[koff[0][k] + ima];
     const real br = pb[koff[1][k]], bi = pb[koff[1][k] + imb];
@@ -279,9 +297,12 @@ __global__ void __launch_bounds__(256) tn_fused_level_kernel(const TnFusedItem* 
   d[MN + idx] = im;
 }
 
+// A circuit with a non-finite parameter returns NaN (the emulated GEMMs run
+// without special-value handling, so such inputs are not propagated there).
 template <typename real>
 __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
-                               real* out, int n_meas, int m, int first, int last) {
+                               real* out, int n_meas, int m, int first, int last, const real* __restrict__ prm,
+                               int n_params) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= batch) return;
   const real* p = root + b * bstride;
@@ -289,7 +310,11 @@ __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, i
   double* a = acc + b * n_meas + m;
   if (!first) v += *a;
   *a = v;
-  if (last) out[b * n_meas + m] = (real)v;
+  if (last) {
+    bool finite = true;
+    for (int j = 0; j < n_params; ++j) finite &= isfinite(prm[b * n_params + j]);
+    out[b * n_meas + m] = finite ? (real)v : (real)NAN;
+  }
 }
 
 }  // namespace
@@ -337,10 +362,10 @@ cudaError_t tn_fused_level(const TnFusedItem* items, int n_items, int blocks, ch
 
 template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
-                    int m, int first, int last, cudaStream_t stream) {
+                    int m, int first, int last, const real* params, int n_params, cudaStream_t stream) {
   const unsigned blocks = (unsigned)((batch + 255) / 256);
   return launch_kernel(tn_root_kernel<real>, dim3(blocks), dim3(256), 0, stream, root, root_bstride, batch, acc, out,
-                       n_meas, m, first, last);
+                       n_meas, m, first, last, params, n_params);
 }
 
 template cudaError_t tn_build_leaves<float>(const TnLeafDesc*, int, const float*, int, int64_t, float*, cudaStream_t);
@@ -353,8 +378,9 @@ template cudaError_t tn_fused<double>(const TnFusedArgs&, cudaStream_t);
 template cudaError_t tn_fused_level<float>(const TnFusedItem*, int, int, char*, const void*, int64_t, cudaStream_t);
 template cudaError_t tn_fused_level<double>(const TnFusedItem*, int, int, char*, const void*, int64_t,
                                             cudaStream_t);
-template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int, cudaStream_t);
+template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int,
+                                    const float*, int, cudaStream_t);
 template cudaError_t tn_root<double>(const double*, int64_t, int64_t, double*, double*, int, int, int, int,
-                                     cudaStream_t);
+                                     const double*, int, cudaStream_t);
 
 }  // namespace tedq

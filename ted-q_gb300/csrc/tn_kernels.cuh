@@ -113,9 +113,10 @@ cudaError_t tn_build_leaves(const TnLeafDesc* desc, int n_desc, const real* para
 template <typename real>
 cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream);
 // acc[b * n_meas + m] (+)= Re(root) for every circuit b (first: assign);
-// last: out[b * n_meas + m] = acc.
+// last: out[b * n_meas + m] = acc (NaN for a circuit with a non-finite
+// parameter).
 template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
-                    int m, int first, int last, cudaStream_t stream);
+                    int m, int first, int last, const real* params, int n_params, cudaStream_t stream);
 
 }  // namespace tedq

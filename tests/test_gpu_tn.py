@@ -147,3 +147,20 @@ def test_tn_level_launch_tables_follow_batch_size():
     for rows in (3, 7, 3, 5):
         got = cc.execute_batch(P[:rows])
         torch.testing.assert_close(got, ones[:rows], atol=2e-6, rtol=1e-5)
+
+
+@pytest.mark.parametrize("gemm", ["bf16x9", "auto", "fp32"])
+def test_tn_non_finite_parameter_gives_nan(gemm):
+    """A circuit with a NaN or infinite parameter returns NaN (as the
+    state-vector path does); the other circuits of the batch are unaffected."""
+    spec = lattice_spec(3, 3, 2, seed=1)
+    cc = _tn(spec, "c64", gemm, requires_grad=False)
+    n = len(flat_params(spec))
+    gen = torch.Generator().manual_seed(1)
+    P = (torch.rand(4, n, generator=gen) * 6.28).to(DEV)
+    clean = cc.execute_batch(P)
+    P[1, 0] = float("nan")
+    P[2, n - 1] = float("inf")
+    got = cc.execute_batch(P)
+    assert torch.isnan(got[1]).all() and torch.isnan(got[2]).all()
+    torch.testing.assert_close(got[[0, 3]], clean[[0, 3]], atol=1e-6, rtol=1e-5)
