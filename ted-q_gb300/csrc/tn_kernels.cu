@@ -143,21 +143,23 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   const int64_t dstride = (o.doubled ? 4 : 2) * n;
   const real* src = static_cast<const real*>(o.src);
   real* dst = static_cast<real*>(o.dst);
-  for (int64_t tile = blockIdx.x; tile < total; tile += gridDim.x) {
+  // software pipeline: the next tile's loads are issued before the current
+  // tile is written out, so each CTA keeps loads in flight across its tiles
+  auto offsets = [&](int64_t tile, int64_t& so, int64_t& dof) {
     const int64_t b = tile >> outer, ou = tile & ((1ll << outer) - 1);
-    int64_t so = o.src_base + b * o.src_bstride + olo_s[ou & ((1 << nlo) - 1)];
-    int64_t dof = b * dstride + olo_d[ou & ((1 << nlo) - 1)];
+    so = o.src_base + b * o.src_bstride + olo_s[ou & ((1 << nlo) - 1)];
+    dof = b * dstride + olo_d[ou & ((1 << nlo) - 1)];
     for (int q = nlo; q < o.n_outer; ++q)
       if ((ou >> q) & 1) {
         so += o.sw[o.outer_bit[q]];
         dof += dw(o.outer_bit[q]);
       }
+  };
+  constexpr int PER = TS_MAX / 256;
+  real vr[PER], vi[PER];
+  int wv[PER];
+  auto load = [&](int64_t so) {
     const real* s = src + so;
-    // all loads of the tile first (up to 4 per thread), then the stores to
-    // shared memory: the loads are in flight together
-    constexpr int PER = TS_MAX / 256;
-    real vr[PER], vi[PER];
-    int wv[PER];
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int r = threadIdx.x + q * 256;
@@ -168,6 +170,13 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
         vi[q] = s[at + o.src_im];
       }
     }
+  };
+  int64_t tile = blockIdx.x, so = 0, dof = 0;
+  if (tile < total) {
+    offsets(tile, so, dof);
+    load(so);
+  }
+  for (; tile < total; tile += gridDim.x) {
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int w = wv[q];
@@ -177,7 +186,12 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
       }
     }
     __syncthreads();
-    real* d = dst + dof;
+    const int64_t dcur = dof;
+    if (tile + gridDim.x < total) {
+      offsets(tile + gridDim.x, so, dof);
+      load(so);
+    }
+    real* d = dst + dcur;
     for (int w = threadIdx.x; w < TS; w += blockDim.x) {
       const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
       real* row = d + dtab[w];
