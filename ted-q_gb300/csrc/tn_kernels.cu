@@ -311,24 +311,28 @@ __global__ void __launch_bounds__(256) tn_fused_level_kernel(const TnFusedItem* 
   d[MN + idx] = im;
 }
 
-// A circuit with a non-finite parameter returns NaN (the emulated GEMMs run
-// without special-value handling, so such inputs are not propagated there).
+// One warp per circuit: lane 0 accumulates the root; on the last slice the
+// warp checks the circuit's parameters (coalesced) and a circuit with a
+// non-finite parameter returns NaN (the emulated GEMMs run without
+// special-value handling, so such inputs are not propagated there).
 template <typename real>
 __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
                                real* out, int n_meas, int m, int first, int last, const real* __restrict__ prm,
                                int n_params) {
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (b >= batch) return;
+  bool finite = true;
+  if (last)
+    for (int j = lane; j < n_params; j += 32) finite &= isfinite(prm[b * n_params + j]);
+  finite = __all_sync(0xffffffffu, finite);
+  if (lane) return;
   const real* p = root + b * bstride;
   double v = (double)p[0];
   double* a = acc + b * n_meas + m;
   if (!first) v += *a;
   *a = v;
-  if (last) {
-    bool finite = true;
-    for (int j = 0; j < n_params; ++j) finite &= isfinite(prm[b * n_params + j]);
-    out[b * n_meas + m] = finite ? (real)v : (real)NAN;
-  }
+  if (last) out[b * n_meas + m] = finite ? (real)v : (real)NAN;
 }
 
 }  // namespace
@@ -377,7 +381,7 @@ cudaError_t tn_fused_level(const TnFusedItem* items, int n_items, int blocks, ch
 template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
                     int m, int first, int last, const real* params, int n_params, cudaStream_t stream) {
-  const unsigned blocks = (unsigned)((batch + 255) / 256);
+  const unsigned blocks = (unsigned)((batch * 32 + 255) / 256);
   return launch_kernel(tn_root_kernel<real>, dim3(blocks), dim3(256), 0, stream, root, root_bstride, batch, acc, out,
                        n_meas, m, first, last, params, n_params);
 }
