@@ -312,7 +312,7 @@ enum {
 typedef struct tedq_tn_options {
   int32_t precision;   /* TEDQ_PREC_C64 / TEDQ_PREC_C128                       */
   int32_t gemm;        /* TEDQ_TN_GEMM_* (complex64 only)                      */
-  int32_t max_rank;    /* 0 = 27                                               */
+  int32_t max_rank;    /* 0 = 27; at most 28                                   */
   int32_t repeats;     /* randomised greedy trials, 0 = 64                     */
   uint64_t seed;       /* 0 = 1                                                */
   int32_t graphs;      /* 1: replay each call's launches as a CUDA graph       */

@@ -525,8 +525,8 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         std::memset(&A, 0, sizeof(A));
         const TnOperand* ops[2] = {&stp.opa, &stp.opb};
         for (int x = 0; x < 2; ++x) {
-          if (ops[x]->nf + ops[x]->nc > kTnMaxBits)
-            return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: operand above 2^48 entries");
+          if (ops[x]->nf + ops[x]->nc > 28)
+            return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: GEMM operand above 2^28 entries (lower max_rank)");
           gather_op(*ops[x], sl, A.op[x]);
         }
         A.op[0].dst = scratch;
@@ -653,7 +653,8 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
         throw std::invalid_argument("unknown precision");
       if (opts->gemm < TEDQ_TN_GEMM_FP32 || opts->gemm > TEDQ_TN_GEMM_AUTO)
         throw std::invalid_argument("unknown GEMM mode");
-      if (opts->max_rank < 0 || opts->max_rank > 34) throw std::invalid_argument("max_rank out of range");
+      // at most 2^28 entries per intermediate (32-bit tile offsets of the gathers)
+      if (opts->max_rank < 0 || opts->max_rank > 28) throw std::invalid_argument("max_rank out of range [0, 28]");
       p->precision = opts->precision;
       p->gemm = opts->gemm;
       p->graphs = opts->graphs != 0;

@@ -96,112 +96,115 @@ __global__ void __launch_bounds__(256) tn_leaf_kernel(const TnLeafDesc* __restri
   }
 }
 
-// Tiled bit-permutation copy (one operand per blockIdx.y, 256 threads): per tile, source
-// elements are read in source order into shared memory (padded one word per
-// 32) and written out in destination order, so both sides are coalesced.
-// Offsets of the tile-local and of the low 8 outer element bits are tabulated
-// once per CTA.
+// Tiled bit-permutation copy (one operand per blockIdx.y, 256 threads): per
+// tile, source elements are read in source order into shared memory (padded
+// one word per 32) and written out in destination order, so both sides are
+// coalesced.  Tile-local offsets are tabulated once per CTA in the order each
+// phase uses them (32-bit: the host limits operands to 2^28 entries), the
+// low 8 outer element bits likewise; the next tile's loads are issued before
+// the current tile is written out.
 template <typename real>
 __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ TnGatherArgs A) {
-  constexpr int TS_MAX = 1 << kTnTileBits;
+  constexpr int TS_MAX = 1 << kTnTileBits, PER = TS_MAX / 256;
   __shared__ real sre[TS_MAX + TS_MAX / 32], sim[TS_MAX + TS_MAX / 32];
-  __shared__ int64_t stab[TS_MAX], dtab[TS_MAX];
+  __shared__ int32_t ld_off[TS_MAX], st_off[TS_MAX];  // read order: source offset; write order: row offset
+  __shared__ int16_t ld_slot[TS_MAX];                 // read order: padded shared-memory slot
   __shared__ int64_t olo_s[256], olo_d[256];
-  __shared__ int16_t r2w_tab[TS_MAX];
-  const TnGatherOp& o = A.op[blockIdx.y];
-  const int tb = o.tb, TS = 1 << tb, nc = o.nc;
-  const int64_t K = 1ll << nc, n = 1ll << o.nbits;
-  auto dw = [&](int j) -> int64_t { return j < nc ? (1ll << j) : ((2 * K) << (j - nc)); };
-  for (int w = threadIdx.x; w < TS; w += blockDim.x) {
-    int64_t so = 0, dof = 0;
-    int rw = 0;
+  const int op = blockIdx.y;
+  const int tb = A.op[op].tb, TS = 1 << tb, nc = A.op[op].nc, nbits = A.op[op].nbits;
+  const int n_outer = A.op[op].n_outer, doubled = A.op[op].doubled;
+  const int64_t K = 1ll << nc, n = 1ll << nbits, src_im = A.op[op].src_im;
+  const int64_t src_bstride = A.op[op].src_bstride, src_base = A.op[op].src_base;
+  const int64_t* sw = A.op[op].sw;
+  const int8_t* tile_bit = A.op[op].tile_bit;
+  const int8_t* r2w = A.op[op].r2w;
+  const int8_t* outer_bit = A.op[op].outer_bit;
+  auto dw = [nc, K](int j) -> int64_t { return j < nc ? (1ll << j) : ((2 * K) << (j - nc)); };
+  for (int r = threadIdx.x; r < TS; r += blockDim.x) {
+    // r as a read-order index: its write-order slot and source offset
+    int w = 0;
+    int64_t so = 0;
     for (int i = 0; i < tb; ++i)
-      if ((w >> i) & 1) {
-        const int j = o.tile_bit[i];
-        so += o.sw[j];
-        dof += dw(j);
-        rw |= 1 << o.r2w[i];
-      }
-    stab[w] = so;
-    dtab[w] = dof;
-    r2w_tab[w] = (int16_t)rw;
+      if ((r >> i) & 1) w |= 1 << r2w[i];
+    for (int i = 0; i < tb; ++i)
+      if ((w >> i) & 1) so += sw[tile_bit[i]];
+    ld_off[r] = (int32_t)so;
+    ld_slot[r] = (int16_t)(w + (w >> 5));
+    // r as a write-order index: its row offset
+    int64_t dof = 0;
+    for (int i = 0; i < tb; ++i)
+      if ((r >> i) & 1) dof += dw(tile_bit[i]);
+    st_off[r] = (int32_t)dof;
   }
-  const int nlo = o.n_outer < 8 ? o.n_outer : 8;
+  const int nlo = n_outer < 8 ? n_outer : 8;
   for (int u = threadIdx.x; u < (1 << nlo); u += blockDim.x) {
     int64_t so = 0, dof = 0;
     for (int q = 0; q < nlo; ++q)
       if ((u >> q) & 1) {
-        so += o.sw[o.outer_bit[q]];
-        dof += dw(o.outer_bit[q]);
+        so += sw[outer_bit[q]];
+        dof += dw(outer_bit[q]);
       }
     olo_s[u] = so;
     olo_d[u] = dof;
   }
   __syncthreads();
-  const int outer = o.nbits - tb;
-  const int64_t total = o.nb << outer;
-  const int64_t dstride = (o.doubled ? 4 : 2) * n;
-  const real* src = static_cast<const real*>(o.src);
-  real* dst = static_cast<real*>(o.dst);
-  // software pipeline: the next tile's loads are issued before the current
-  // tile is written out, so each CTA keeps loads in flight across its tiles
-  auto offsets = [&](int64_t tile, int64_t& so, int64_t& dof) {
-    const int64_t b = tile >> outer, ou = tile & ((1ll << outer) - 1);
-    so = o.src_base + b * o.src_bstride + olo_s[ou & ((1 << nlo) - 1)];
-    dof = b * dstride + olo_d[ou & ((1 << nlo) - 1)];
-    for (int q = nlo; q < o.n_outer; ++q)
-      if ((ou >> q) & 1) {
-        so += o.sw[o.outer_bit[q]];
-        dof += dw(o.outer_bit[q]);
-      }
-  };
-  constexpr int PER = TS_MAX / 256;
+  const int outer = nbits - tb;
+  const int64_t total = A.op[op].nb << outer;
+  const int64_t dstride = (doubled ? 4 : 2) * n;
+  const real* __restrict__ src = static_cast<const real*>(A.op[op].src);
+  real* __restrict__ dst = static_cast<real*>(A.op[op].dst);
+  const int lomask = (1 << nlo) - 1;
   real vr[PER], vi[PER];
-  int wv[PER];
-  auto load = [&](int64_t so) {
-    const real* s = src + so;
+  int64_t tile = blockIdx.x, dcur = 0;
+  auto load = [&](int64_t t) {
+    const int64_t b = t >> outer, ou = t & ((1ll << outer) - 1);
+    int64_t so = src_base + b * src_bstride + olo_s[ou & lomask];
+    int64_t dof = b * dstride + olo_d[ou & lomask];
+    for (int q = nlo; q < n_outer; ++q)
+      if ((ou >> q) & 1) {
+        so += sw[outer_bit[q]];
+        dof += dw(outer_bit[q]);
+      }
+    const real* sp = src + so;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
       const int r = threadIdx.x + q * 256;
-      wv[q] = r < TS ? r2w_tab[r] : 0;
       if (r < TS) {
-        const int64_t at = stab[wv[q]];
-        vr[q] = s[at];
-        vi[q] = s[at + o.src_im];
+        const int32_t at = ld_off[r];
+        vr[q] = sp[at];
+        vi[q] = sp[at + src_im];
       }
     }
+    return dof;
   };
-  int64_t tile = blockIdx.x, so = 0, dof = 0;
-  if (tile < total) {
-    offsets(tile, so, dof);
-    load(so);
-  }
+  if (tile < total) dcur = load(tile);
   for (; tile < total; tile += gridDim.x) {
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-      const int w = wv[q];
-      if (threadIdx.x + q * 256 < TS) {
-        sre[w + (w >> 5)] = vr[q];
-        sim[w + (w >> 5)] = vi[q];
+      const int r = threadIdx.x + q * 256;
+      if (r < TS) {
+        const int slot = ld_slot[r];
+        sre[slot] = vr[q];
+        sim[slot] = vi[q];
       }
     }
     __syncthreads();
-    const int64_t dcur = dof;
-    if (tile + gridDim.x < total) {
-      offsets(tile + gridDim.x, so, dof);
-      load(so);
-    }
     real* d = dst + dcur;
-    for (int w = threadIdx.x; w < TS; w += blockDim.x) {
-      const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
-      real* row = d + dtab[w];
-      row[0] = re;
-      if (!o.doubled) {
-        row[K] = im;
-      } else {
-        row[K] = -im;
-        row[n * 2] = im;  // row F + f
-        row[n * 2 + K] = re;
+    if (tile + gridDim.x < total) dcur = load(tile + gridDim.x);
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int w = threadIdx.x + q * 256;
+      if (w < TS) {
+        const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
+        real* row = d + st_off[w];
+        row[0] = re;
+        if (!doubled) {
+          row[K] = im;
+        } else {
+          row[K] = -im;
+          row[2 * n] = im;  // row F + f
+          row[2 * n + K] = re;
+        }
       }
     }
     __syncthreads();
@@ -353,6 +356,7 @@ cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
   for (int i = 0; i < 2; ++i) {
     const TnGatherOp& o = args.op[i];
     if (o.tb < 0 || o.tb > kTnTileBits || o.tb > o.nbits || o.n_outer != o.nbits - o.tb) return cudaErrorInvalidValue;
+    if (o.nbits > 28) return cudaErrorInvalidValue;  // 32-bit tile tables
     const int64_t t = o.nb << (o.nbits - o.tb);
     most = t > most ? t : most;
   }
