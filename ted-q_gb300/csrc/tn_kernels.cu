@@ -120,21 +120,27 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   const int8_t* r2w = A.op[op].r2w;
   const int8_t* outer_bit = A.op[op].outer_bit;
   auto dw = [nc, K](int j) -> int64_t { return j < nc ? (1ll << j) : ((2 * K) << (j - nc)); };
+  // tables by doubling: entry x | 2^i = entry x + weight of bit i
+  __shared__ int16_t wr[TS_MAX];  // read-order index -> write-order index
+  if (threadIdx.x == 0) {
+    ld_off[0] = 0;
+    st_off[0] = 0;
+    wr[0] = 0;
+  }
+  __syncthreads();
+  for (int i = 0; i < tb; ++i) {
+    const int h = 1 << i;
+    const int32_t wsrc = (int32_t)sw[tile_bit[r2w[i]]], wdst = (int32_t)dw(tile_bit[i]);
+    for (int x = threadIdx.x; x < h; x += blockDim.x) {
+      ld_off[h + x] = ld_off[x] + wsrc;
+      st_off[h + x] = st_off[x] + wdst;
+      wr[h + x] = (int16_t)(wr[x] | (1 << r2w[i]));
+    }
+    __syncthreads();
+  }
   for (int r = threadIdx.x; r < TS; r += blockDim.x) {
-    // r as a read-order index: its write-order slot and source offset
-    int w = 0;
-    int64_t so = 0;
-    for (int i = 0; i < tb; ++i)
-      if ((r >> i) & 1) w |= 1 << r2w[i];
-    for (int i = 0; i < tb; ++i)
-      if ((w >> i) & 1) so += sw[tile_bit[i]];
-    ld_off[r] = (int32_t)so;
+    const int w = wr[r];
     ld_slot[r] = (int16_t)(w + (w >> 5));
-    // r as a write-order index: its row offset
-    int64_t dof = 0;
-    for (int i = 0; i < tb; ++i)
-      if ((r >> i) & 1) dof += dw(tile_bit[i]);
-    st_off[r] = (int32_t)dof;
   }
   const int nlo = n_outer < 8 ? n_outer : 8;
   for (int u = threadIdx.x; u < (1 << nlo); u += blockDim.x) {
@@ -360,8 +366,10 @@ cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
     const int64_t t = o.nb << (o.nbits - o.tb);
     most = t > most ? t : most;
   }
+  // about one resident wave over both operands (6 CTAs of 256 threads per SM):
+  // the per-CTA tables are built once for many tiles
   int64_t blocks = most;
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > 152 * 3) blocks = 152 * 3;
   return launch_kernel(tn_gather_kernel<real>, dim3((unsigned)blocks, 2), dim3(256), 0, stream, args);
 }
 
