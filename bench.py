@@ -692,7 +692,7 @@ def run_tn(a):
             "gpu_launches": int(per_call),
             "roofline": {"bound": "tensor",
                          "kernel": "contractions: fused in-place kernels (small) + cuBLAS strided-batched GEMMs "
-                                   "(4M real embedding; BF16x9 tensor cores for >= 2^24 flops per circuit)",
+                                   "(4M real embedding; BF16x9 tensor cores for >= 2^20 flops per circuit)",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if peak else None, "traffic": None, "peak_kind": peak_kind,
                          "gemm_ms_per_step": prof.gemm_ms / a.steps, "gather_ms_per_step": prof.gather_ms / a.steps,

@@ -305,7 +305,7 @@ enum {
   TEDQ_TN_GEMM_BF16X9 = 1,  /* FP32 accuracy from BF16 tensor-core products
                                (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9)    */
   TEDQ_TN_GEMM_TF32 = 2,    /* one TF32 product per term (~1e-3 relative)     */
-  TEDQ_TN_GEMM_AUTO = 3     /* BF16x9 for the large contractions (at least 2^24
+  TEDQ_TN_GEMM_AUTO = 3     /* BF16x9 for the large contractions (at least 2^20
                                flops per circuit), FP32 for the rest          */
 };
 

@@ -397,8 +397,9 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
          : p->gemm == TEDQ_TN_GEMM_BF16X9 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
                                           : CUBLAS_COMPUTE_32F;
   // AUTO: BF16x9 on the tensor cores for contractions of at least 2^auto_log2
-  // real flops per circuit, FP32 below
-  int auto_log2 = 24;
+  // real flops per circuit, FP32 below (measured on the 6x6 lattice: 2^20 to
+  // 2^22 best once the emulation runs without special-value passes)
+  int auto_log2 = 20;
   if (const char* env = getenv("TEDQ_GB300_TN_AUTO_LOG2")) auto_log2 = atoi(env);
   const real one = 1, zero = 0;
   const int n_meas = (int)p->nets.size();

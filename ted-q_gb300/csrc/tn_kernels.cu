@@ -366,10 +366,10 @@ cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream) {
     const int64_t t = o.nb << (o.nbits - o.tb);
     most = t > most ? t : most;
   }
-  // about one resident wave over both operands (6 CTAs of 256 threads per SM):
-  // the per-CTA tables are built once for many tiles
+  // several CTAs per SM per operand: each keeps one tile of loads in flight
+  // (fewer, longer-lived CTAs measured slower)
   int64_t blocks = most;
-  if (blocks > 152 * 3) blocks = 152 * 3;
+  if (blocks > 152 * 8) blocks = 152 * 8;
   return launch_kernel(tn_gather_kernel<real>, dim3((unsigned)blocks, 2), dim3(256), 0, stream, args);
 }
 
