@@ -458,6 +458,9 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       }
       for (int j = 0; j < o.nbits; ++j)
         if (std::find(tile.begin(), tile.end(), j) == tile.end()) o.outer_bit[o.n_outer++] = (int8_t)j;
+      // vector access (every offset involved is even, see TnGatherOp)
+      o.rmode = T.leaf >= 0 ? 2 : ((o.tb >= 1 && o.sw[rd[0]] == 1 && T.lm >= 1) ? 1 : 0);
+      o.wpair = (o.nc >= 1 && o.tb >= 1) ? 1 : 0;
     };
     // fused operand: per-bit offsets (reals) of the source storage
     auto fused_op = [&](const TnOperand& op, int64_t sl, TnFusedOp& o) {

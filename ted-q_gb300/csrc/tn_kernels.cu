@@ -12,6 +12,8 @@
 // doubled operand).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "launch.cuh"
 #include "tedq_gb300.h"
 #include "tn_kernels.cuh"
@@ -162,6 +164,8 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   const int lomask = (1 << nlo) - 1;
   real vr[PER], vi[PER];
   int64_t tile = blockIdx.x, dcur = 0;
+  using V2 = typename std::conditional<sizeof(real) == 4, float2, double2>::type;
+  const int rmode = A.op[op].rmode, wpair = A.op[op].wpair;
   auto load = [&](int64_t t) {
     const int64_t b = t >> outer, ou = t & ((1ll << outer) - 1);
     int64_t so = src_base + b * src_bstride + olo_s[ou & lomask];
@@ -172,44 +176,104 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
         dof += dw(outer_bit[q]);
       }
     const real* sp = src + so;
+    if (rmode == 1) {
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int r = threadIdx.x + q * 256;
-      if (r < TS) {
-        const int32_t at = ld_off[r];
-        vr[q] = sp[at];
-        vi[q] = sp[at + src_im];
+      for (int q = 0; q < PER / 2; ++q) {
+        const int r = 2 * (threadIdx.x + q * 256);
+        if (r < TS) {
+          const int32_t at = ld_off[r];
+          const V2 a = *reinterpret_cast<const V2*>(sp + at);
+          const V2 c = *reinterpret_cast<const V2*>(sp + at + src_im);
+          vr[2 * q] = a.x;
+          vr[2 * q + 1] = a.y;
+          vi[2 * q] = c.x;
+          vi[2 * q + 1] = c.y;
+        }
+      }
+    } else if (rmode == 2) {
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int r = threadIdx.x + q * 256;
+        if (r < TS) {
+          const V2 a = *reinterpret_cast<const V2*>(sp + ld_off[r]);
+          vr[q] = a.x;
+          vi[q] = a.y;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int r = threadIdx.x + q * 256;
+        if (r < TS) {
+          const int32_t at = ld_off[r];
+          vr[q] = sp[at];
+          vi[q] = sp[at + src_im];
+        }
       }
     }
     return dof;
   };
   if (tile < total) dcur = load(tile);
   for (; tile < total; tile += gridDim.x) {
+    if (rmode == 1) {
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int r = threadIdx.x + q * 256;
-      if (r < TS) {
-        const int slot = ld_slot[r];
-        sre[slot] = vr[q];
-        sim[slot] = vi[q];
+      for (int q = 0; q < PER / 2; ++q) {
+        const int r = 2 * (threadIdx.x + q * 256);
+        if (r < TS) {
+          const int s0 = ld_slot[r], s1 = ld_slot[r + 1];
+          sre[s0] = vr[2 * q];
+          sim[s0] = vi[2 * q];
+          sre[s1] = vr[2 * q + 1];
+          sim[s1] = vi[2 * q + 1];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int r = threadIdx.x + q * 256;
+        if (r < TS) {
+          const int slot = ld_slot[r];
+          sre[slot] = vr[q];
+          sim[slot] = vi[q];
+        }
       }
     }
     __syncthreads();
     real* d = dst + dcur;
     if (tile + gridDim.x < total) dcur = load(tile + gridDim.x);
+    if (wpair) {
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-      const int w = threadIdx.x + q * 256;
-      if (w < TS) {
-        const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
-        real* row = d + st_off[w];
-        row[0] = re;
-        if (!doubled) {
-          row[K] = im;
-        } else {
-          row[K] = -im;
-          row[2 * n] = im;  // row F + f
-          row[2 * n + K] = re;
+      for (int q = 0; q < PER / 2; ++q) {
+        const int w = 2 * (threadIdx.x + q * 256);
+        if (w < TS) {
+          const int s0 = w + (w >> 5), s1 = (w + 1) + ((w + 1) >> 5);
+          const real r0 = sre[s0], r1 = sre[s1], i0 = sim[s0], i1 = sim[s1];
+          real* row = d + st_off[w];
+          *reinterpret_cast<V2*>(row) = V2{r0, r1};
+          if (!doubled) {
+            *reinterpret_cast<V2*>(row + K) = V2{i0, i1};
+          } else {
+            *reinterpret_cast<V2*>(row + K) = V2{-i0, -i1};
+            *reinterpret_cast<V2*>(row + 2 * n) = V2{i0, i1};  // row F + f
+            *reinterpret_cast<V2*>(row + 2 * n + K) = V2{r0, r1};
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const int w = threadIdx.x + q * 256;
+        if (w < TS) {
+          const real re = sre[w + (w >> 5)], im = sim[w + (w >> 5)];
+          real* row = d + st_off[w];
+          row[0] = re;
+          if (!doubled) {
+            row[K] = im;
+          } else {
+            row[K] = -im;
+            row[2 * n] = im;  // row F + f
+            row[2 * n + K] = re;
+          }
         }
       }
     }

@@ -42,7 +42,11 @@ struct TnGatherOp {
   int64_t src_im;       // reals from the real to the imaginary part
   int64_t nb;           // batch entries gathered (1 for a shared operand)
   int64_t sw[kTnMaxBits];
-  int32_t nbits, nc, doubled, tb, n_outer, pad;
+  int32_t nbits, nc, doubled, tb, n_outer;
+  // vector access: rmode 0 = scalar reads, 1 = two adjacent elements per
+  // thread (unit source weight on the lowest read bit), 2 = (re, im) pairs of
+  // interleaved leaves; wpair = two adjacent elements per store (nc >= 1)
+  int8_t rmode, wpair, pad[2];
   int8_t tile_bit[kTnTileBits];
   int8_t r2w[kTnTileBits];
   int8_t outer_bit[kTnMaxBits];
