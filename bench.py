@@ -720,7 +720,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--qubits", type=int, default=20)
     ap.add_argument("--layers", type=int, default=10)
-    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--batch", type=int, default=None, help="circuits per step (default 4096 for small8, else 1024)")
     ap.add_argument("--plain", action="store_true", help="unfused per-gate passes")
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
@@ -735,6 +735,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     a = ap.parse_args()
+    if a.batch is None:
+        a.batch = 4096 if a.workload == "small8" else 1024
     if a.impl == "reference":
         return run_reference_arm(a)
     if a.workload == "serving":
