@@ -265,8 +265,10 @@ __device__ void factor_mat(const PassParams& P, const Factor& F, const real* prm
 
 // Matrix i of a pass: product of its factors (first factor applied first),
 // conjugate-transposed for the adjoint sweep.  Diagonal matrices keep 2 entries.
+// norm = false (generic kernels): normalised rotations keep their plain
+// entries and run as GK_RXT / GK_RYT.
 template <typename real>
-__device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<real>* out) {
+__device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<real>* out, bool norm = true) {
   const MatDesc md = P.mat[i];
   cpx<real> M[4], F[4], T[4];
   factor_mat<real>(P, P.factor[md.f0], prm, M);
@@ -288,7 +290,7 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
     M[0] = cconj(M[0]);
     M[3] = cconj(M[3]);
   }
-  if (md.diag >= 3) {  // normalised rotation: divide by the larger of |c|, |s|
+  if (md.diag >= 3 && norm) {  // normalised rotation: divide by the larger of |c|, |s|
     const real c = M[0].x, sn = md.diag == 3 ? -M[1].y : -M[1].x;
     const bool f0 = fabs(c) >= fabs(sn);
     out[0] = mk<real>(f0 ? sn / c : c / sn, f0 ? (real)0 : (real)1);
@@ -299,7 +301,7 @@ __device__ void compute_mat(const PassParams& P, int i, const real* prm, cpx<rea
   if (md.diag == 2) {  // unit-modulus diagonal: d1 / d0 = d1 conj(d0)
     out[0] = mk<real>((real)1, (real)0);
     out[1] = cmul(M[3], cconj(M[0]));
-  } else if (md.diag) {
+  } else if (md.diag == 1) {
     out[0] = M[0];
     out[1] = M[3];
   } else {
@@ -935,8 +937,6 @@ __device__ __forceinline__ void dispatch_gate(int kind, int k, Regs<real, R>& a,
         case GK_RYT: apply_ryt<K, R, real>(a, M, cm); break;
         case GK_PH: apply_ph<K, R, real>(a, M, cm); break;
         case GK_H: apply_h<K, R, real>(a, cm); break;
-        case GK_RXN: apply_rxn<K, R, real>(a, M); break;
-        case GK_RYN: apply_ryn<K, R, real>(a, M); break;
         default: apply_x<K, R, real>(a, cm); break;
       }
     } else {
@@ -945,9 +945,13 @@ __device__ __forceinline__ void dispatch_gate(int kind, int k, Regs<real, R>& a,
   }
 }
 
+// Generic kernels: normalised rotations arrive with plain entries
+// (compute_mat with norm = false) and run as RX / RY-type gates.
 template <int R, typename real>
 __device__ __forceinline__ void apply_rgate(const RGate& r, Regs<real, R>& a, const cpx<real>* M) {
-  if (r.kind == GK_SWAP) {
+  if (r.kind == GK_RXN || r.kind == GK_RYN) {
+    dispatch_gate<R, real>(r.kind == GK_RXN ? GK_RXT : GK_RYT, r.k0, a, M, r.cmask);
+  } else if (r.kind == GK_SWAP) {
     const unsigned b0 = 1u << r.k0, b1 = 1u << r.k1;
     dispatch_gate<R, real>(GK_X, r.k1, a, M, r.cmask | b0);
     dispatch_gate<R, real>(GK_X, r.k0, a, M, r.cmask | b1);
@@ -1088,7 +1092,7 @@ struct FwdPass {
   Regs<real, R> a;
 
   __device__ __forceinline__ FwdPass(const PassParams& P_, S* tile_, C (*mats_)[4], C* psi, const real* params,
-                                     int n_params, const C* init, int64_t circ0)
+                                     int n_params, const C* init, int64_t circ0, bool norm = true)
       : P(P_), tile(tile_), mats(mats_) {
     tid = threadIdx.x;
     const int T = blockDim.x;
@@ -1102,8 +1106,8 @@ struct FwdPass {
 #pragma unroll
     for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
     // matrices while the tile loads are in flight
-    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
-    if (P.norm_last != kNoNorm) {
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
+    if (norm && P.norm_last != kNoNorm) {
       __syncthreads();
       norm_scan<real>(P, mats, tid);
     }
@@ -1168,7 +1172,8 @@ struct BwdPass {
   Regs<real, R> l;
 
   __device__ __forceinline__ BwdPass(const PassParams& P_, S* smem, C (*mats_)[4], double* gacc_, C* psi, C* lam,
-                                     const real* params, int n_params_, double* grad_acc_, int64_t circ0)
+                                     const real* params, int n_params_, double* grad_acc_, int64_t circ0,
+                                     bool norm = true)
       : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_) {
     tid = threadIdx.x;
     const int T = blockDim.x;
@@ -1178,8 +1183,8 @@ struct BwdPass {
     sp = psi + (circ << P.n);
     sl = lam + (circ << P.n);
     const real* prm = params ? params + circ * n_params : nullptr;
-    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i]);
-    if (P.norm_last != kNoNorm) {
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
+    if (norm && P.norm_last != kNoNorm) {
       __syncthreads();
       norm_scan<real>(P, mats, tid);
     }
@@ -1643,6 +1648,19 @@ struct BwdPassP {
 }  // namespace tedq
 
 // Kernel prologues shared by the generic and the generated pass kernels.
+// Generic (interpreted) kernels: plain matrices for the normalised rotations.
+#define TEDQ_FWD_PROLOGUE_GENERIC(REAL, RB)                                                          \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
+  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
+                                 psi, params, n_params, init, circ0, false);
+#define TEDQ_BWD_PROLOGUE_GENERIC(REAL, RB)                                                          \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
+  __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                              \
+  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
+                                 tedq_gacc, psi, lam, params, n_params, grad_acc, circ0, false);
+
 #define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                  \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \

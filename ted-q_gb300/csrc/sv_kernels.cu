@@ -48,13 +48,14 @@ constexpr int kE = dev::UnitsPerAmp<real>::E;
 // ---------------------------------------------------------------- pass kernels
 // Generic pass kernels: the gates of each phase are dispatched at run time
 // from the PassParams tables (used when no specialised kernel was generated).
+// Normalised rotations run with their plain matrices here (no pass scale).
 
 template <typename real, int R>
 __global__ void __launch_bounds__(256, 2)
     fwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi,
                     const real* __restrict__ params, int n_params, const cpx<real>* __restrict__ init,
                     int64_t circ0) {
-  TEDQ_FWD_PROLOGUE(real, R)
+  TEDQ_FWD_PROLOGUE_GENERIC(real, R)
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
     if (ph.type == PH_REG) {
@@ -63,7 +64,6 @@ __global__ void __launch_bounds__(256, 2)
         const RGate& r = P.gate[g];
         dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
       }
-      if (f == P.norm_phase) dev::rescale<R>(c.a, c.mats[P.norm_last][2].x);
       c.end(f);
     } else {
       c.dense(f);
@@ -76,28 +76,16 @@ template <typename real, int R>
 __global__ void __launch_bounds__(256, 2)
     bwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi, cpx<real>* __restrict__ lam,
                     const real* __restrict__ params, int n_params, double* __restrict__ grad_acc, int64_t circ0) {
-  TEDQ_BWD_PROLOGUE(real, R)
-  int kap = kNoNorm;  // last normalised matrix applied in this pass
+  TEDQ_BWD_PROLOGUE_GENERIC(real, R)
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
     if (ph.type == PH_REG) {
       c.begin(f);
       for (int g = ph.g0; g < ph.g1; ++g) {
         const RGate& r = P.gate[g];
-        if (r.grad != GR_NONE) {
-          // both states carry 1 / (scale so far): the product carries its square
-          real v = dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask);
-          if (kap != kNoNorm) v *= dev::sq(c.mats[kap][2].x);
-          c.grad(g, v);
-        }
+        if (r.grad != GR_NONE) c.grad(g, dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask));
         dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
         dev::apply_rgate<R, real>(r, c.l, c.mats[r.mat]);
-        if (r.kind == GK_RXN || r.kind == GK_RYN) kap = r.mat;
-      }
-      if (f == P.norm_phase) {
-        dev::rescale<R>(c.a, c.mats[P.norm_last][2].x);
-        dev::rescale<R>(c.l, c.mats[P.norm_last][2].x);
-        kap = kNoNorm;
       }
       c.end(f);
     } else {

@@ -890,7 +890,13 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   const bool norm_f = norm_opt.find('f') != std::string::npos, norm_b = norm_opt.find('b') != std::string::npos,
              norm_u = norm_opt.find('u') != std::string::npos;
   p->normalise = !p->persist && (norm_f || norm_b);
-  if (p->fuse) p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && !p->persist && norm_f && norm_u);
+  // unfusing pays only in specialised kernels: the generic ones dispatch every
+  // gate at run time (and run normalised rotations with plain matrices)
+  const int jit_mode = opts ? opts->jit : 0;
+  const char* jit_env = getenv("TEDQ_GB300_JIT");
+  const bool jit_expected = (jit_mode > 0 || (jit_mode == 0 && p->ns >= 14)) && !(jit_env && jit_env[0] == '0');
+  if (p->fuse)
+    p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && !p->persist && norm_f && norm_u && jit_expected);
   p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, !p->persist && norm_f);
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
   p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, !p->persist && norm_b);
