@@ -1132,6 +1132,14 @@ struct FwdPass {
     __syncthreads();
   }
 
+  // end of a phase whose successor is warp-local (Phase::wlocal)
+  __device__ __forceinline__ void end_w(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
+    __syncwarp();
+  }
+
   __device__ __forceinline__ void dense(int f) {
     dense_phase<real>(P, P.phase[f], tile, tid, blockDim.x);
     __syncthreads();
@@ -1226,6 +1234,17 @@ struct BwdPass {
       tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
     }
     __syncthreads();
+  }
+
+  // end of a phase whose successor is warp-local (Phase::wlocal)
+  __device__ __forceinline__ void end_w(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
+      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
+    }
+    __syncwarp();
   }
 
   // Warp-reduce one gate's partial gradient into this warp's slot of gate g

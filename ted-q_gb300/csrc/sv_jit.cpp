@@ -156,7 +156,8 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
       if (adjoint) o << "  rescale<" << (int)P.R << ">(c.l, c.mats[" << (int)P.norm_last << "][2].x);\n";
       kap = -1;
     }
-    o << "  c.end(" << f << ");\n";
+    const bool next_wl = !persist && f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal;
+    o << (next_wl ? "  c.end_w(" : "  c.end(") << f << ");\n";
   }
   o << (persist ? "  c.finish();\n  }\n}\n\n" : "  c.finish();\n}\n\n");
 }

@@ -64,7 +64,8 @@ __global__ void __launch_bounds__(256, 2)
         const RGate& r = P.gate[g];
         dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
       }
-      c.end(f);
+      if (f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
+      else c.end(f);
     } else {
       c.dense(f);
     }
@@ -87,7 +88,8 @@ __global__ void __launch_bounds__(256, 2)
         dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
         dev::apply_rgate<R, real>(r, c.l, c.mats[r.mat]);
       }
-      c.end(f);
+      if (f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
+      else c.end(f);
     } else {
       c.dense(f);
     }

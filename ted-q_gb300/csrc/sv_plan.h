@@ -122,7 +122,10 @@ struct Phase {
   uint8_t dpos[3];     // tile positions, dpos[0] = most significant matrix bit
   uint16_t dcmask;     // control mask over tile positions
   uint8_t dagger;
-  uint8_t pad;
+  // PH_REG: 1 = every warp touches the same shared-memory units as in the
+  // previous register phase (same warp-index bits, the lane and register bits
+  // permuted among themselves), so the transition needs only __syncwarp
+  uint8_t wlocal;
   uint16_t dfix;       // first entry in fixed[] (4^dk entries, row-major)
   uint16_t pad2;
 };

@@ -514,6 +514,10 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
   const uint32_t forced = (1u << G.e) - 1;
   std::vector<int> rem = taken;
   rejected.clear();
+  // warp-index tile positions of the previous register phase (thread bits 5
+  // and up; empty after a dense phase): kept as the warp bits of the next
+  // phase where they stay thread bits, so that transition is warp-local
+  std::vector<int> prev_warp;
   while (!rem.empty()) {
     if ((int)P.n_phases == kMaxPhases) {
       rejected = rem;
@@ -530,6 +534,7 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       ph.dfix = (uint16_t)push_fixed(first.dmat.data(), (int)first.dmat.size());
       P.n_phases++;
       rem.erase(rem.begin());
+      prev_warp.clear();
       continue;
     }
     uint32_t Rset = forced, blocked = 0;
@@ -551,36 +556,63 @@ static void build_pass(PassParams& P, const Geometry& G, int ns, uint64_t L, con
       }
     }
     // fill the register set: keep every residue class of (pos - e) mod 3
-    // represented among the thread bits so lanes 0..2 can be conflict-free.
+    // represented among the thread bits so lanes 0..2 can be conflict-free,
+    // and leave the previous phase's warp bits to the threads where possible
+    uint32_t pw = 0;
+    for (int p : prev_warp) pw |= 1u << p;
     while (popc(Rset) < G.R) {
       int cnt[3] = {0, 0, 0};
       for (int p = G.e; p < G.m; ++p)
         if (!(Rset >> p & 1)) cnt[(p - G.e) % 3]++;
       int best = -1;
-      for (int p = G.e; p < G.m; ++p) {
-        if (Rset >> p & 1) continue;
-        if (best < 0 || cnt[(p - G.e) % 3] > cnt[(best - G.e) % 3]) best = p;
-      }
+      for (int pass = 0; pass < 2 && best < 0; ++pass)
+        for (int p = G.e; p < G.m; ++p) {
+          if (Rset >> p & 1) continue;
+          if (pass == 0 && (pw >> p & 1)) continue;
+          if (best < 0 || cnt[(p - G.e) % 3] > cnt[(best - G.e) % 3]) best = p;
+        }
       Rset |= 1u << best;
     }
     std::vector<int> Rpos = sorted_bits(Rset);
     int regbit_of[32];
     for (int i = 0; i < 32; ++i) regbit_of[i] = -1;
     for (size_t i = 0; i < Rpos.size(); ++i) regbit_of[Rpos[i]] = (int)i;
-    // thread bits: lanes 0..2 from distinct residue classes, then the rest
-    std::vector<int> tpos;
-    std::vector<int> free_pos;
-    for (int p = 0; p < G.m; ++p)
-      if (!(Rset >> p & 1)) free_pos.push_back(p);
-    for (int cls = 0; cls < 3; ++cls)
-      for (size_t i = 0; i < free_pos.size(); ++i)
-        if (free_pos[i] >= 0 && (free_pos[i] - G.e) % 3 == cls) {
-          tpos.push_back(free_pos[i]);
-          free_pos[i] = -1;
-          break;
-        }
-    for (int p : free_pos)
-      if (p >= 0) tpos.push_back(p);
+    // thread bits: lanes 0..2 from distinct residue classes, then the rest;
+    // when the previous phase's warp bits are all thread bits here, they keep
+    // their warp-index positions (bits 5 and up) and lanes 0..4 come from
+    // the other positions
+    auto order_tid = [&](bool keep_warp) {
+      std::vector<int> t, free_pos;
+      for (int p = 0; p < G.m; ++p)
+        if (!(Rset >> p & 1) && !(keep_warp && (pw >> p & 1))) free_pos.push_back(p);
+      for (int cls = 0; cls < 3; ++cls)
+        for (size_t i = 0; i < free_pos.size(); ++i)
+          if (free_pos[i] >= 0 && (free_pos[i] - G.e) % 3 == cls) {
+            t.push_back(free_pos[i]);
+            free_pos[i] = -1;
+            break;
+          }
+      for (int p : free_pos)
+        if (p >= 0) t.push_back(p);
+      if (keep_warp) t.insert(t.end(), prev_warp.begin(), prev_warp.end());
+      return t;
+    };
+    const int ntid_all = G.m - G.R;
+    bool wl = !prev_warp.empty() && (int)prev_warp.size() == ntid_all - 5 && !(Rset & pw);
+    auto classes = [&](const std::vector<int>& t) {
+      int seen = 0;
+      for (int b = 0; b < 3 && b < (int)t.size(); ++b) seen |= 1 << ((t[b] - G.e + 3) % 3);
+      return popc(seen);
+    };
+    std::vector<int> tpos = order_tid(false);
+    if (wl) {
+      // only if lanes 0..2 cover as many residue classes as without the constraint
+      std::vector<int> tw = order_tid(true);
+      if (classes(tw) >= classes(tpos)) tpos = tw;
+      else wl = false;
+    }
+    ph.wlocal = wl ? 1 : 0;
+    prev_warp.assign(tpos.begin() + std::min<size_t>(5, tpos.size()), tpos.end());
     ph.type = PH_REG;
     ph.ntid = (uint8_t)tpos.size();
     for (size_t b = 0; b < tpos.size(); ++b) ph.tid_off[b] = (uint16_t)swz_unit((1u << tpos[b]) >> G.e);
@@ -934,7 +966,7 @@ std::string describe_schedule(const Program& p, bool adjoint) {
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];
       if (f) o << ",";
-      o << "{\"type\":" << (int)ph.type;
+      o << "{\"type\":" << (int)ph.type << ",\"wlocal\":" << (int)ph.wlocal;
       if (ph.type == PH_REG) {
         o << ",\"reg_off\":[";
         for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << ph.reg_off[j];

@@ -218,3 +218,45 @@ def test_plan_register_gate_forms(monkeypatch, norm):
         dy = np.asarray(case["dy"], dtype=np.float64)
         g = plan_interp.adjoint(bwd, prm, psi.copy(), dy[:fwd["n_real"]], None)
         np.testing.assert_allclose(g, case["grad_backprop_c128"], atol=1e-10, rtol=1e-9)
+
+
+def _warp_units(ph, e, R, warp):
+    units = set()
+    for lane in range(32):
+        tid = warp * 32 + lane
+        bu = 0
+        for b, off in enumerate(ph["tid_off"]):
+            if (tid >> b) & 1:
+                bu ^= off
+        for j in range(1 << (R - e)):
+            units.add(bu ^ ph["reg_off"][j])
+    return units
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+@pytest.mark.parametrize("n,layers", [(14, 3), (20, 10)])
+def test_plan_warp_local_transitions(n, layers, adjoint):
+    """A register phase marked warp-local touches, in every warp, exactly the
+    shared-memory units the warp touched in the previous register phase (the
+    kernels then separate the two phases with __syncwarp only)."""
+    spec = _hea_spec(n, layers, seed=n)
+    desc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300").describe(adjoint=adjoint)
+    marked = total = 0
+    for P in desc["passes"]:
+        e, R = P["e"], P["R"]
+        nwarps = 1 << max(0, len(P["phases"][0].get("tid_off", [])) - 5) if P["phases"] else 1
+        prev = None
+        for ph in P["phases"]:
+            if ph["type"] != 0:
+                assert not ph.get("wlocal")
+                prev = None
+                continue
+            if prev is not None:
+                total += 1
+            if ph["wlocal"]:
+                assert prev is not None
+                marked += 1
+                for w in range(1 << (len(ph["tid_off"]) - 5)):
+                    assert _warp_units(prev, e, R, w) == _warp_units(ph, e, R, w)
+            prev = ph
+    assert total == 0 or marked > 0
