@@ -346,7 +346,11 @@ int64_t tedq_tn_plan_describe(const tedq_tn_plan_t* plan, char* buf, int64_t len
 int64_t tedq_tn_workspace_bytes(const tedq_tn_plan_t* plan, int64_t batch);
 /* params    [batch][n_params] float (c64) / double (c128), device
  * out       [batch][n_meas]   float / double, device
- * workspace >= tedq_tn_workspace_bytes(batch) bytes, device, 256-byte aligned */
+ * workspace >= tedq_tn_workspace_bytes(batch) bytes, device, 256-byte aligned
+ * The first call with a new batch size uploads the plan's table of small
+ * contractions for that size (synchronising the device): make one call with
+ * a batch size before capturing calls with it in a CUDA graph.  A circuit
+ * with a non-finite parameter returns NaN. */
 int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch, void* out,
                          void* workspace, size_t workspace_bytes, void* stream);
 
