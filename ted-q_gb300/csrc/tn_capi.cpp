@@ -667,8 +667,10 @@ int32_t tedq_tn_plan_create(const tedq_gate_t* gates, int32_t n_gates, int32_t n
       if (opts->seed) po.seed = opts->seed;
     }
     // tuning; at most 13 keeps every fused operand within the level-launch
-    // item limits (12 free, 8 contracted bits)
+    // item limits (16 free, 8 contracted bits)
     if (const char* env = getenv("TEDQ_GB300_TN_FUSED_LOG2")) po.fused_log2 = std::max(0, std::min(13, atoi(env)));
+    if (const char* env = getenv("TEDQ_GB300_TN_SHORT_LOG2"))  // tuning, -1 = off
+      po.fused_short_log2 = std::max(-1, std::min(8, atoi(env)));
     p->n = n_qubits;
     for (int i = 0; i < n_gates && gates; ++i)
       for (int j = 0; j < 3; ++j) p->n_params = std::max(p->n_params, gates[i].param_slot[j] + 1);

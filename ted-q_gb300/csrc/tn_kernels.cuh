@@ -90,7 +90,7 @@ cudaError_t tn_fused(const TnFusedArgs& args, cudaStream_t stream);
 // slice weights of the sliced indices set in the current slice) and its
 // imaginary part `im` reals further; the result is planar (Re at j * M + i,
 // Im at + M * N).
-constexpr int kTnItemFree = 12, kTnItemSum = 8, kTnItemSlice = 6;
+constexpr int kTnItemFree = 16, kTnItemSum = 8, kTnItemSlice = 6;
 struct TnFusedItem {
   int64_t off[2];      // operand a / b
   int64_t bstride[2];  // 0: shared by all circuits

@@ -116,6 +116,9 @@ struct TnNet {
 
 struct TnPlanOptions {
   int fused_log2 = 13;  // contractions below 2^fused_log2 complex MACs per circuit run fused
+  // ... and so do contractions over at most 2^fused_short_log2 terms with up
+  // to 2^16 outputs per circuit (a short sum per output: memory-bound, no GEMM)
+  int fused_short_log2 = 3;
   int max_rank = 27;   // slice until every intermediate has at most 2^max_rank entries
   int repeats = 64;    // randomised greedy trials (the first is plain greedy)
   uint64_t seed = 1;
