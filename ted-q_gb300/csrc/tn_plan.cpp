@@ -561,7 +561,7 @@ TnNet tn_build(const tedq_gate_t* gates, int n_gates, int n_qubits, const tedq_m
       const int lm = (int)st.free_a.size(), ln = (int)st.free_b.size(), lk = (int)st.contracted.size();
       // small contractions with enough outputs (or a short sum) per circuit
       st.fused = (lm + ln + lk < opt.fused_log2 && lk <= 8 && (lm + ln >= 5 || lk <= 6)) ||
-                 (lk <= opt.fused_short_log2 && lm <= 16 && ln <= 16 && lm + ln <= 16);
+                 (opt.fused_short_log2 >= 0 && lk <= opt.fused_short_log2 && lm + ln <= 16);
       if (st.fused) st.double_a = false;
     }
     int lv = 0;

@@ -116,9 +116,11 @@ struct TnNet {
 
 struct TnPlanOptions {
   int fused_log2 = 13;  // contractions below 2^fused_log2 complex MACs per circuit run fused
-  // ... and so do contractions over at most 2^fused_short_log2 terms with up
-  // to 2^16 outputs per circuit (a short sum per output: memory-bound, no GEMM)
-  int fused_short_log2 = 3;
+  // ... and, when >= 0, contractions over at most 2^fused_short_log2 terms
+  // with up to 2^16 outputs per circuit.  Off: on the 6x6 lattice the in-place
+  // kernel ran those slower than gather + GEMM (uncoalesced operand reads;
+  // 258k vs 283k contractions/s with 3)
+  int fused_short_log2 = -1;
   int max_rank = 27;   // slice until every intermediate has at most 2^max_rank entries
   int repeats = 64;    // randomised greedy trials (the first is plain greedy)
   uint64_t seed = 1;
