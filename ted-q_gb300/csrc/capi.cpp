@@ -331,13 +331,12 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
       P.init = init ? 2 : 1;
       P.pad_bits = (uint8_t)p.pad;
       e = timed(prog, 0, batch << p.ns, s, [&] {
-        return jk ? jit_launch_fwd(jk->fwd[0], dbl, P, psi, params, p.n_params, init, batch, s, p.persist)
+        return jk ? jit_launch_fwd(jk->fwd[0], dbl, P, psi, params, p.n_params, init, batch, s)
                   : launch_fwd_pass(dbl, P, psi, params, p.n_params, init, batch, s);
       });
     } else {
       e = timed(prog, 0, batch << p.ns, s, [&] {
-        return jk ? jit_launch_fwd(jk->fwd[i], dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s,
-                                   p.persist)
+        return jk ? jit_launch_fwd(jk->fwd[i], dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s)
                   : launch_fwd_pass(dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s);
       });
     }
@@ -405,7 +404,7 @@ int32_t tedq_run_adjoint(tedq_program_t* prog, const void* params, int64_t batch
   for (size_t i = 0; i < p.bwd.passes.size(); ++i) {
     const PassParams& P = p.bwd.passes[i];
     e = timed(prog, 1, batch << p.ns, s, [&] {
-      return jk ? jit_launch_bwd(jk->bwd[i], dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s, p.persist)
+      return jk ? jit_launch_bwd(jk->bwd[i], dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s)
                 : launch_bwd_pass(dbl, P, psi, lambda_, params, p.n_params, grad_acc, batch, s);
     });
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run_adjoint/pass");

@@ -1320,349 +1320,6 @@ struct BwdPass {
   }
 };
 
-// ---------------------------------------------------------------- persistent passes
-// A persistent CTA walks a contiguous range of (circuit, tile) items.  While
-// the register phases of item i run on one shared-memory buffer, the tile of
-// item i+1 streams into the other with cp.async, so HBM traffic overlaps the
-// phases of the CTA itself.  Units arrive in their global (interleaved)
-// format and each thread converts the units it copied once they are in.
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-// shared-memory unit in place: global format -> pair-planar
-__device__ __forceinline__ void unit_to_s(SUnit<float>* u) {
-  const Unit<float> g = *reinterpret_cast<const Unit<float>*>(u);
-  *u = to_s(g);
-}
-__device__ __forceinline__ void unit_to_s(SUnit<double>*) {}
-
-// Item range of this CTA: a contiguous share of n_items.
-struct ItemRange {
-  int64_t item, end;
-  __device__ __forceinline__ ItemRange(int64_t n_items) {
-    const int64_t G = gridDim.x, j = blockIdx.x, q = n_items / G, r = n_items % G;
-    item = j * q + (j < r ? j : r);
-    end = item + q + (j < r ? 1 : 0);
-  }
-};
-
-template <typename real, int R>
-struct FwdPassP {
-  using C = cpx<real>;
-  using U = Unit<real>;
-  using S = SUnit<real>;
-  static constexpr int E = UnitsPerAmp<real>::E;
-  static constexpr int NR = 1 << R;
-  static constexpr int NU = NR >> E;
-  const PassParams& P;
-  S* buf0;
-  S* buf1;
-  S* tile;
-  C (*mats)[4];
-  C* psi;
-  const real* params;
-  int n_params;
-  const C* init;
-  int tid, cur;
-  bool started;
-  ItemRange rg;
-  int64_t mats_circ;
-  uint64_t gtid;  // thread part of the global offset
-  uint32_t sthr;
-  uint64_t gthr;  // current item: tile base | thread part
-  C* st;          // current circuit's state
-  uint32_t bu;
-  Regs<real, R> a;
-
-  __device__ __forceinline__ FwdPassP(const PassParams& P_, S* smem, C (*mats_)[4], C* psi_, const real* params_,
-                                      int n_params_, const C* init_, int64_t n_items)
-      : P(P_), mats(mats_), psi(psi_), params(params_), n_params(n_params_), init(init_), rg(n_items) {
-    tid = threadIdx.x;
-    buf0 = smem;
-    buf1 = smem + (1 << (P.m - E));
-    cur = 0;
-    started = false;
-    mats_circ = -1;
-    gtid = 0;
-    sthr = 0;
-    thread_offsets(P, tid, P.m - R, gtid, sthr);
-  }
-
-  // Starts the copy of item's tile into b (global format).
-  __device__ __forceinline__ void issue(int64_t item, S* b) {
-    const int64_t circ = item >> (P.n - P.m);
-    const uint64_t g = tile_base(P, (uint32_t)(item & ((1ll << (P.n - P.m)) - 1))) | gtid;
-    const C* s = psi + (circ << P.n);
-    if (P.init == 0) {
-#pragma unroll
-      for (int k = 0; k < NU; ++k)
-        cp_async16(&b[sthr ^ P.sk[k]], reinterpret_cast<const U*>(s) + ((g | P.gk[k]) >> E));
-    } else {
-#pragma unroll
-      for (int k = 0; k < NU; ++k)
-        *reinterpret_cast<U*>(&b[sthr ^ P.sk[k]]) = load_unit<real>(P, s, g | P.gk[k], init);
-    }
-    cp_async_commit();
-  }
-
-  // Next item: false when the range is done.  On return the item's tile is in
-  // `tile` (pair-planar) and the matrices are those of its circuit.
-  __device__ __forceinline__ bool next() {
-    if (!started) {
-      started = true;
-      if (rg.item >= rg.end) return false;
-      issue(rg.item, buf0);
-    } else {
-      ++rg.item;
-      cur ^= 1;
-      if (rg.item >= rg.end) return false;
-    }
-    const bool more = rg.item + 1 < rg.end;
-    if (more) {
-      issue(rg.item + 1, cur ? buf0 : buf1);
-      cp_async_wait_1();
-    } else {
-      cp_async_wait_0();
-    }
-    tile = cur ? buf1 : buf0;
-#pragma unroll
-    for (int k = 0; k < NU; ++k) unit_to_s(&tile[sthr ^ P.sk[k]]);
-    const int64_t circ = rg.item >> (P.n - P.m);
-    gthr = tile_base(P, (uint32_t)(rg.item & ((1ll << (P.n - P.m)) - 1))) | gtid;
-    st = psi + (circ << P.n);
-    if (circ != mats_circ) {
-      const real* prm = params ? params + circ * n_params : nullptr;
-      for (int i = tid; i < P.n_mats; i += blockDim.x) compute_mat<real>(P, i, prm, mats[i]);
-      mats_circ = circ;
-    }
-    __syncthreads();
-    return true;
-  }
-
-  __device__ __forceinline__ void begin(int f) {
-    const Phase& ph = P.phase[f];
-    bu = 0;
-    for (int b = 0; b < ph.ntid; ++b)
-      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) regs_ld(a, j, tile[bu ^ ph.reg_off[j]]);
-  }
-
-  __device__ __forceinline__ void end(int f) {
-    const Phase& ph = P.phase[f];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
-    __syncthreads();
-  }
-
-  __device__ __forceinline__ void dense(int f) {
-    dense_phase<real>(P, P.phase[f], tile, tid, blockDim.x);
-    __syncthreads();
-  }
-
-  // Tile back to HBM; the buffer is free for the copy after the next one.
-  __device__ __forceinline__ void finish() {
-    U* gst = reinterpret_cast<U*>(st);
-#pragma unroll
-    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = from_s(tile[sthr ^ P.sk[k]]);
-    __syncthreads();
-  }
-};
-
-template <typename real, int R, int NW>
-struct BwdPassP {
-  using C = cpx<real>;
-  using U = Unit<real>;
-  using S = SUnit<real>;
-  static constexpr int E = UnitsPerAmp<real>::E;
-  static constexpr int NR = 1 << R;
-  static constexpr int NU = NR >> E;
-  const PassParams& P;
-  S* bp0;
-  S* bl0;
-  S* bp1;
-  S* bl1;
-  S* tp;
-  S* tl;
-  C (*mats)[4];
-  double* gacc;
-  C* psi;
-  C* lam;
-  const real* params;
-  int n_params;
-  double* grad_acc;
-  int tid, cur;
-  bool started;
-  ItemRange rg;
-  int64_t circ, mats_circ;
-  uint64_t gtid;
-  uint32_t sthr;
-  uint64_t gthr;
-  C* sp;
-  C* sl;
-  uint32_t bu;
-  Regs<real, R> a;
-  Regs<real, R> l;
-
-  __device__ __forceinline__ BwdPassP(const PassParams& P_, S* smem, C (*mats_)[4], double* gacc_, C* psi_, C* lam_,
-                                      const real* params_, int n_params_, double* grad_acc_, int64_t n_items)
-      : P(P_), mats(mats_), gacc(gacc_), psi(psi_), lam(lam_), params(params_), n_params(n_params_),
-        grad_acc(grad_acc_), rg(n_items) {
-    tid = threadIdx.x;
-    const int units = 1 << (P.m - E);
-    bp0 = smem;
-    bl0 = smem + units;
-    bp1 = smem + 2 * units;
-    bl1 = smem + 3 * units;
-    cur = 0;
-    started = false;
-    mats_circ = -1;
-    gtid = 0;
-    sthr = 0;
-    thread_offsets(P, tid, P.m - R, gtid, sthr);
-  }
-
-  __device__ __forceinline__ void issue(int64_t item, S* p, S* q) {
-    const int64_t c = item >> (P.n - P.m);
-    const uint64_t g = tile_base(P, (uint32_t)(item & ((1ll << (P.n - P.m)) - 1))) | gtid;
-    const U* s1 = reinterpret_cast<const U*>(psi + (c << P.n));
-    const U* s2 = reinterpret_cast<const U*>(lam + (c << P.n));
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      cp_async16(&p[sthr ^ P.sk[k]], s1 + ((g | P.gk[k]) >> E));
-      cp_async16(&q[sthr ^ P.sk[k]], s2 + ((g | P.gk[k]) >> E));
-    }
-    cp_async_commit();
-  }
-
-  __device__ __forceinline__ bool next() {
-    if (!started) {
-      started = true;
-      if (rg.item >= rg.end) return false;
-      issue(rg.item, bp0, bl0);
-    } else {
-      ++rg.item;
-      cur ^= 1;
-      if (rg.item >= rg.end) return false;
-    }
-    const bool more = rg.item + 1 < rg.end;
-    if (more) {
-      issue(rg.item + 1, cur ? bp0 : bp1, cur ? bl0 : bl1);
-      cp_async_wait_1();
-    } else {
-      cp_async_wait_0();
-    }
-    tp = cur ? bp1 : bp0;
-    tl = cur ? bl1 : bl0;
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      unit_to_s(&tp[sthr ^ P.sk[k]]);
-      unit_to_s(&tl[sthr ^ P.sk[k]]);
-    }
-    circ = rg.item >> (P.n - P.m);
-    gthr = tile_base(P, (uint32_t)(rg.item & ((1ll << (P.n - P.m)) - 1))) | gtid;
-    sp = psi + (circ << P.n);
-    sl = lam + (circ << P.n);
-    if (circ != mats_circ) {
-      const real* prm = params ? params + circ * n_params : nullptr;
-      for (int i = tid; i < P.n_mats; i += blockDim.x) compute_mat<real>(P, i, prm, mats[i]);
-      mats_circ = circ;
-    }
-    __syncthreads();
-    return true;
-  }
-
-  __device__ __forceinline__ void begin(int f) {
-    const Phase& ph = P.phase[f];
-    bu = 0;
-    for (int b = 0; b < ph.ntid; ++b)
-      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) {
-      regs_ld(a, j, tp[bu ^ ph.reg_off[j]]);
-      regs_ld(l, j, tl[bu ^ ph.reg_off[j]]);
-    }
-  }
-
-  __device__ __forceinline__ void end(int f) {
-    const Phase& ph = P.phase[f];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) {
-      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
-      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
-    }
-    __syncthreads();
-  }
-
-  // Eight gates at once (see BwdPass::grad8).
-  __device__ __forceinline__ void grad8(real v0, real v1, real v2, real v3, real v4, real v5, real v6, real v7,
-                                        int g0, int g1, int g2, int g3, int g4, int g5, int g6, int g7) {
-    const unsigned lane = tid & 31;
-    real v[8] = {v0, v1, v2, v3, v4, v5, v6, v7};
-    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const real send = b4 ? v[j] : v[j + 4];
-      const real keep = b4 ? v[j + 4] : v[j];
-      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const real send = b3 ? v[j] : v[j + 2];
-      const real keep = b3 ? v[j + 2] : v[j];
-      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-    {
-      const real send = b2 ? v[0] : v[1];
-      const real keep = b2 ? v[1] : v[0];
-      v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-    if ((lane & 3) == 0) {
-      const int which = (b4 ? 4 : 0) + (b3 ? 2 : 0) + (b2 ? 1 : 0);
-      const int gs[8] = {g0, g1, g2, g3, g4, g5, g6, g7};
-      int g = gs[0];
-#pragma unroll
-      for (int j = 1; j < 8; ++j)
-        if (which == j) g = gs[j];
-      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = (double)v[0];
-    }
-  }
-
-  __device__ __forceinline__ void dense(int f) {
-    dense_phase<real>(P, P.phase[f], tp, tid, blockDim.x);
-    dense_phase<real>(P, P.phase[f], tl, tid, blockDim.x);
-    __syncthreads();
-  }
-
-  __device__ __forceinline__ void finish() {
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      const uint64_t g = (gthr | P.gk[k]) >> E;
-      reinterpret_cast<U*>(sp)[g] = from_s(tp[sthr ^ P.sk[k]]);
-      reinterpret_cast<U*>(sl)[g] = from_s(tl[sthr ^ P.sk[k]]);
-    }
-    if (P.n_grad) {
-      __syncthreads();
-      for (int g = tid; g < P.n_gates; g += blockDim.x) {
-        const int32_t slot = P.gate[g].slot;
-        if (slot < 0) continue;
-        double sum = 0.0;
-        for (int w = 0; w < NW; ++w) sum += gacc[w * kMaxPassGates + g];
-        atomicAdd(&grad_acc[circ * n_params + slot], sum * (double)P.gate[g].coef);
-      }
-    }
-    __syncthreads();
-  }
-};
-
 }  // namespace dev
 }  // namespace tedq
 
@@ -1692,18 +1349,3 @@ struct BwdPassP {
   __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                                  \
   tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);
-
-// Prologues of the persistent generated kernels (kernel argument n_items =
-// circuits x tiles per circuit; NW = warps per CTA).
-#define TEDQ_FWDP_PROLOGUE(REAL, RB)                                                                  \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                      \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                       \
-  tedq::dev::FwdPassP<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
-                                  psi, params, n_params, init, n_items);
-
-#define TEDQ_BWDP_PROLOGUE(REAL, RB, NW)                                                              \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                      \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                       \
-  __shared__ double tedq_gacc[(NW) * tedq::kMaxPassGates];                                            \
-  tedq::dev::BwdPassP<REAL, RB, NW> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw),    \
-                                      tedq_mats, tedq_gacc, psi, lam, params, n_params, grad_acc, n_items);

@@ -69,32 +69,17 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
   }
 }
 
-static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint, bool persist) {
+static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
   // as many CTAs per SM as their shared memory (tile + matrices + gradient
   // slots) allows while every thread may keep 128 registers
   const int threads = 1 << (P.m - P.R);
-  const int tile_bytes = ((adjoint ? 32 : 16) << (P.m - P.e)) * (persist ? 2 : 1);
+  const int tile_bytes = (adjoint ? 32 : 16) << (P.m - P.e);
   const int static_bytes = adjoint ? 5 * 1024 + (threads / 32) * kMaxPassGates * 8 : 5 * 1024;
   int min_blocks = std::min((227 * 1024) / (tile_bytes + static_bytes), 65536 / (threads * 128));
   min_blocks = std::max(1, std::min(min_blocks, 8));
-  if (persist && !adjoint) {
-    snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
-             "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
-             "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init,\n"
-             "    long long n_items) {\n"
-             "  TEDQ_FWDP_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
-             threads, min_blocks, index, real, real, real, real, P.R);
-  } else if (persist) {
-    snprintf(buf, sizeof buf,
-             "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_bwd_%d(\n"
-             "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
-             "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long n_items) {\n"
-             "  TEDQ_BWDP_PROLOGUE(%s, %d, %d)\n  while (c.next()) {\n",
-             threads, min_blocks, index, real, real, real, real, P.R, threads / 32);
-  } else if (!adjoint) {
+  if (!adjoint) {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
@@ -156,10 +141,10 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
       if (adjoint) o << "  rescale<" << (int)P.R << ">(c.l, c.mats[" << (int)P.norm_last << "][2].x);\n";
       kap = -1;
     }
-    const bool next_wl = !persist && f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal;
+    const bool next_wl = f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal;
     o << (next_wl ? "  c.end_w(" : "  c.end(") << f << ");\n";
   }
-  o << (persist ? "  c.finish();\n  }\n}\n\n" : "  c.finish();\n}\n\n");
+  o << "  c.finish();\n}\n\n";
 }
 
 std::vector<JitSource> jit_sources(const Program& p) {
@@ -169,7 +154,7 @@ std::vector<JitSource> jit_sources(const Program& p) {
     o << "// generated by tedq_gb300: specialised pass kernel of one compiled circuit\n"
          "#include \"sv_device.cuh\"\n"
          "using namespace tedq;\nusing namespace tedq::dev;\n\n";
-    emit_pass(o, P, i, adjoint, p.persist);
+    emit_pass(o, P, i, adjoint);
     out.push_back({(adjoint ? "tedq_bwd_" : "tedq_fwd_") + std::to_string(i), o.str()});
   };
   for (size_t i = 0; i < p.fwd.passes.size(); ++i) one(p.fwd.passes[i], (int)i, false);
@@ -370,7 +355,6 @@ struct Driver {
   decltype(&cuModuleGetFunction) get = nullptr;
   decltype(&cuFuncSetAttribute) set_attr = nullptr;
   decltype(&cuLaunchKernel) launch = nullptr;
-  decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
 };
 
 template <typename F>
@@ -389,8 +373,7 @@ bool entry(const char* name, F& fn, std::string& why) {
 Driver load_driver() {
   Driver d;
   if (!entry("cuModuleLoadData", d.load, d.why) || !entry("cuModuleGetFunction", d.get, d.why) ||
-      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why) ||
-      !entry("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy, d.why))
+      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why))
     return d;
   d.ok = true;
   return d;
@@ -404,23 +387,6 @@ Driver& driver() {
 }
 
 constexpr int kMaxGridY = 65535;
-
-// Resident CTAs of a persistent kernel on the whole device (cached per kernel).
-int persistent_grid(void* fn, int threads, size_t smem) {
-  static std::mutex mu;
-  static std::vector<std::pair<void*, int>> cache;
-  std::lock_guard<std::mutex> lk(mu);
-  for (auto& e : cache)
-    if (e.first == fn) return e.second;
-  int per_sm = 0, dev = 0, sms = 0;
-  if (driver().occupancy(&per_sm, reinterpret_cast<CUfunction>(fn), threads, smem) != CUDA_SUCCESS || per_sm < 1)
-    per_sm = 1;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
-                                                 cudaSuccess)
-    sms = 1;
-  cache.push_back({fn, per_sm * sms});
-  return per_sm * sms;
-}
 
 }  // namespace
 
@@ -462,17 +428,9 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
 static cudaError_t to_rt(CUresult r) { return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure; }
 
 cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
-                           const void* init, int64_t batch, cudaStream_t s, bool persist) {
+                           const void* init, int64_t batch, cudaStream_t s) {
   const int E = dbl ? 0 : 1;
   const unsigned smem = 16u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
-  if (persist) {
-    long long n_items = batch << (P.n - P.m);
-    const unsigned grid = (unsigned)std::min<long long>(n_items, persistent_grid(fn, (int)T, 2 * smem));
-    void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
-                    const_cast<void**>(&init), &n_items};
-    return to_rt(driver().launch(reinterpret_cast<CUfunction>(fn), grid, 1, 1, T, 1, 1, 2 * smem,
-                                 reinterpret_cast<CUstream>(s), args, nullptr));
-  }
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     long long circ0 = c0;
@@ -486,17 +444,9 @@ cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, c
 }
 
 cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
-                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s, bool persist) {
+                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
   const int E = dbl ? 0 : 1;
   const unsigned smem = 32u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
-  if (persist) {
-    long long n_items = batch << (P.n - P.m);
-    const unsigned grid = (unsigned)std::min<long long>(n_items, persistent_grid(fn, (int)T, 2 * smem));
-    void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
-                    &n_items};
-    return to_rt(driver().launch(reinterpret_cast<CUfunction>(fn), grid, 1, 1, T, 1, 1, 2 * smem,
-                                 reinterpret_cast<CUstream>(s), args, nullptr));
-  }
   for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
     const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
     long long circ0 = c0;

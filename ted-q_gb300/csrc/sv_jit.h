@@ -42,11 +42,11 @@ struct JitKernels {
 bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSource>& srcs, int n_fwd, int n_bwd,
               JitKernels& out, std::string& err);
 
-// persist: the kernels were generated in the persistent form (grid = resident
-// CTAs, each walking a range of (circuit, tile) items).
+// One launch per pass: grid = (tiles of a state, circuits), chunked by the
+// grid's y limit.
 cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
-                           const void* init, int64_t batch, cudaStream_t s, bool persist);
+                           const void* init, int64_t batch, cudaStream_t s);
 cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
-                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s, bool persist);
+                           int n_params, double* grad_acc, int64_t batch, cudaStream_t s);
 
 }  // namespace tedq

@@ -878,14 +878,6 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   gf.e = gb.e = dbl ? 0 : 1;
   gf.R = dbl ? 4 : 5;
   gb.R = dbl ? 3 : 4;
-  // persistent kernels double-buffer their tile: one bit smaller tiles keep
-  // three CTAs per SM
-  const char* persist_env = getenv("TEDQ_GB300_PERSIST");
-  p->persist = !dbl && persist_env && persist_env[0] == '1';
-  if (p->persist) {
-    mdef_f -= 1;
-    mdef_b -= 1;
-  }
   gf.m = std::min(mdef_f, p->ns);
   gb.m = std::min(mdef_b, p->ns);
   // tuning override "fwd_m,fwd_R,bwd_m,bwd_R" (0 keeps a default); tile and
@@ -913,25 +905,25 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   bool state_out = opts && opts->exact_phase;
   for (int i = 0; i < n_meas; ++i) state_out |= meas[i].kind == TEDQ_MEAS_STATE;
   p->phase_free = !state_out;
-  // normalised rotations (one FMA per component; the persistent kernels do
-  // not track the pass scale).  Tuning: TEDQ_GB300_NORMALISE holds the
-  // letters f (forward passes), b (adjoint passes), u (runs of one-qubit
-  // gates stay unfused where their normalised parts cost less); "0" = none.
+  // normalised rotations (one FMA per component).  Tuning:
+  // TEDQ_GB300_NORMALISE holds the letters f (forward passes), b (adjoint
+  // passes), u (runs of one-qubit gates stay unfused where their normalised
+  // parts cost less); "0" = none.
   const char* norm_env = getenv("TEDQ_GB300_NORMALISE");
   const std::string norm_opt = norm_env ? norm_env : "fbu";
   const bool norm_f = norm_opt.find('f') != std::string::npos, norm_b = norm_opt.find('b') != std::string::npos,
              norm_u = norm_opt.find('u') != std::string::npos;
-  p->normalise = !p->persist && (norm_f || norm_b);
+  p->normalise = norm_f || norm_b;
   // unfusing pays only in specialised kernels: the generic ones dispatch every
   // gate at run time (and run normalised rotations with plain matrices)
   const int jit_mode = opts ? opts->jit : 0;
   const char* jit_env = getenv("TEDQ_GB300_JIT");
   const bool jit_expected = (jit_mode > 0 || (jit_mode == 0 && p->ns >= 14)) && !(jit_env && jit_env[0] == '0');
   if (p->fuse)
-    p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && !p->persist && norm_f && norm_u && jit_expected);
-  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, !p->persist && norm_f);
+    p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && norm_f && norm_u && jit_expected);
+  p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, norm_f);
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
-  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, !p->persist && norm_b);
+  p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, norm_b);
   compile_measurements(*p, meas, n_meas);
   for (auto& pr : p->probs)
     if ((int)pr.bits.size() < p->n) p->n_probs_bins += 1 << pr.bits.size();

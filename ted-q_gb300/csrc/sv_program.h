@@ -62,7 +62,6 @@ struct Program {
   int precision = TEDQ_PREC_C64;
   int fuse = 1;
   int tile_qubits = 0;
-  bool persist = false;  // persistent pass kernels with asynchronous tile prefetch
   bool phase_free = false;  // forward passes may drop global phases (no state output)
   bool normalise = false;   // normalised RX / RY register gates (GK_RXN / GK_RYN)
   std::vector<HGate> elem;    // elementary gates, circuit order
