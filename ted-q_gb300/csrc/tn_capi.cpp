@@ -99,6 +99,14 @@ inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // ---------------------------------------------------------------------- plan
 
+// One level launch: the fused steps [step0, step1) of a network (same level).
+struct TnLevelRun {
+  int step0 = 0, step1 = 0;
+  int item0 = 0, n_items = 0;
+  int blocks = 0;
+  double flops = 0;
+};
+
 struct TnDevice {
   bool ready = false;
   cublasHandle_t handle = nullptr;
@@ -115,14 +123,7 @@ struct TnDevice {
   TnFusedItem* items = nullptr;
   size_t items_cap = 0;
   int64_t items_batch = -1;
-};
-
-// One level launch: the fused steps [step0, step1) of a network (same level).
-struct TnLevelRun {
-  int step0 = 0, step1 = 0;
-  int item0 = 0, n_items = 0;
-  int blocks = 0;
-  double flops = 0;
+  std::vector<std::vector<TnLevelRun>> runs;  // per network, for items_batch
 };
 
 struct tedq_tn_plan {
@@ -135,7 +136,6 @@ struct tedq_tn_plan {
   int64_t const_total = 0, desc_total = 0;
   std::mutex mu;
   TnDevice dev[64];
-  std::vector<std::vector<TnLevelRun>> runs;  // per network, for the current item table
   // kernel timing (tedq_tn_profile_*)
   struct Ev {
     cudaEvent_t a, b;
@@ -254,7 +254,7 @@ int32_t prepare_items(tedq_tn_plan* p, TnDevice& D, int64_t batch) {
   const Layout L = layout(p, batch);
   const int64_t es = elem_bytes(p);
   std::vector<TnFusedItem> items;
-  p->runs.assign(p->nets.size(), {});
+  D.runs.assign(p->nets.size(), {});
   for (size_t m = 0; m < p->nets.size(); ++m) {
     const TnNet& net = p->nets[m];
     const int64_t cb = p->const_base[m];
@@ -329,13 +329,13 @@ int32_t prepare_items(tedq_tn_plan* p, TnDevice& D, int64_t batch) {
           one.step0 = (int)k;
           one.step1 = (int)k + 1;
           one.n_items = 0;
-          p->runs[m].push_back(one);
+          D.runs[m].push_back(one);
         }
       } else {
         run.step1 = (int)j;
         run.n_items = (int)(j - i);
         run.blocks = (int)blocks;
-        p->runs[m].push_back(run);
+        D.runs[m].push_back(run);
       }
       i = j;
     }
@@ -486,7 +486,7 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       for (int j = 0; j < op.nf; ++j) o.wf[j] = w(op.src_bit[op.nc + j]);
     };
     const int64_t n_slices = 1ll << net.sliced.size();
-    const std::vector<TnLevelRun>& runs = p->runs[m];
+    const std::vector<TnLevelRun>& runs = D.runs[m];
     for (int64_t sl = 0; sl < n_slices; ++sl) {
       size_t next_run = 0;
       for (size_t si = 0; si < net.steps.size(); ++si) {
