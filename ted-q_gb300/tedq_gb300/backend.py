@@ -51,12 +51,32 @@ def _cmatrix(m, k):
     return np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1).reshape(-1))
 
 
+class _Projector:
+    """|0><0| / |1><1| on one qubit as matrix observables (outcome
+    probabilities of the tensor-network mode)."""
+
+    class _P:
+        def __init__(self, q, b):
+            self.qubits = [q]
+            self.name = "Projector"
+            self.matrix = np.diag([1.0 - b, float(b)]).astype(np.complex128)
+
+    def __init__(self, q):
+        self._p = (self._P(q, 0), self._P(q, 1))
+
+    def at(self, b):
+        return self._p[b]
+
+
 class _Recorded:
     """C-ABI arrays (``tedq_gate_t``, ``tedq_meas_t``) of a recorded circuit,
     with the positional binding of trainable parameters to slots
     (compiled_circuit.py:492-547)."""
 
-    def __init__(self, circuit):
+    # largest probs(qubits=...) of the tensor-network mode: one network per outcome
+    TN_MAX_PROBS_QUBITS = 8
+
+    def __init__(self, circuit, tn=False):
         self.n = int(circuit.num_qubits)
         ops = list(circuit.operators)
         gates = (_lib.Gate * max(1, len(ops)))()
@@ -126,6 +146,14 @@ class _Recorded:
             k_real += 1
             return k_real - 1
 
+        def add_projector_expvals(qs):
+            """probs over the sorted qubits qs as expectation values of the
+            projector products |x><x| (outcome x: the first qubit is the most
+            significant bit, as in pytorch_backend.py:461-472)."""
+            proj = [_Projector(q) for q in qs]
+            for x in range(2 ** len(qs)):
+                add_expval([proj[i].at((x >> (len(qs) - 1 - i)) & 1) for i in range(len(qs))])
+
         for m in meas:
             kind = _kind(m)
             obs = (m.obs if isinstance(m.obs, list) else [m.obs]) if m.obs is not None else []
@@ -134,6 +162,17 @@ class _Recorded:
             elif kind == "var":
                 # <O^2> - <O>^2 from two native expectation values
                 self.layout.append(("var", add_expval(obs), add_expval(obs, square=True)))
+            elif kind == "probs" and tn:
+                # the tensor-network mode contracts one network per outcome
+                qs = sorted(set(int(q) for q in (range(self.n) if m.qubits is None else m.qubits)))
+                if len(qs) == 0:
+                    raise ValueError("probs(qubits=[]) has no outcome")
+                if len(qs) > self.TN_MAX_PROBS_QUBITS:
+                    raise NotImplementedError(f"the tensor-network mode evaluates probs over at most "
+                                              f"{self.TN_MAX_PROBS_QUBITS} qubits (one network per outcome)")
+                k0 = k_real
+                add_projector_expvals(qs)
+                self.layout.append(("probs", k0, len(qs), m))
             elif kind == "probs":
                 if m.qubits is None:
                     native.append((_lib.MEAS_PROBS, None, 0, None, 0))
@@ -239,9 +278,10 @@ class NativeTnPlan:
         L = _lib.lib()
         if circuit.init_state is not None:
             raise NotImplementedError("the tensor-network mode starts from |0...0>")
-        rec = _Recorded(circuit)
-        if any(item[0] != "expval" for item in rec.layout):
-            raise NotImplementedError("the tensor-network mode evaluates expectation values only")
+        rec = _Recorded(circuit, tn=True)
+        if any(item[0] not in ("expval", "var", "probs") for item in rec.layout):
+            raise NotImplementedError("the tensor-network mode evaluates expectation values, variances and "
+                                      "outcome probabilities only")
         if gemm not in _lib.TN_GEMM:
             raise ValueError(f"tn_gemm must be one of {sorted(_lib.TN_GEMM)}")
         self._rec = rec

@@ -164,3 +164,22 @@ def test_tn_non_finite_parameter_gives_nan(gemm):
     got = cc.execute_batch(P)
     assert torch.isnan(got[1]).all() and torch.isnan(got[2]).all()
     torch.testing.assert_close(got[[0, 3]], clean[[0, 3]], atol=1e-6, rtol=1e-5)
+
+
+def test_tn_probs_match_state_vector():
+    """probs(qubits=...) in the tensor-network mode (one network per outcome)
+    agrees with the state-vector path, values and parameter-shift gradients."""
+    spec = hea_spec(8, 3)
+    spec["meas"] = [{"kind": "probs", "qubits": [5, 2]}]
+    tn = _tn(spec, "c64", "fp32")
+    sv = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300")
+    n = len(flat_params(spec))
+    gen = torch.Generator().manual_seed(7)
+    P = (torch.rand(3, n, generator=gen) * 6.28).to(DEV)
+    torch.testing.assert_close(tn.execute_batch(P), sv.execute_batch(P), atol=2e-6, rtol=1e-5)
+    p1 = P[0].clone().requires_grad_(True)
+    p2 = P[0].clone().requires_grad_(True)
+    w = torch.arange(4, dtype=torch.float32, device=DEV).reshape(1, 2, 2)
+    (tn(p1) * w).sum().backward()
+    (sv(p2) * w).sum().backward()
+    torch.testing.assert_close(p1.grad, p2.grad, atol=2e-5, rtol=1e-4)

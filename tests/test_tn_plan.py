@@ -193,11 +193,36 @@ def test_tn_capi_rejects_probs_and_bad_input():
     assert L.tedq_tn_plan_destroy(h) == _lib.OK
 
 
-def test_tn_mode_rejects_non_expval():
+def test_tn_mode_rejects_state_and_wide_probs():
     spec = random_spec(1)
-    spec["meas"] = [{"kind": "probs", "qubits": [0]}]
+    spec["meas"] = [{"kind": "state"}]
     with pytest.raises(NotImplementedError):
         plan(spec)
+    spec = random_spec(2, n=10)
+    spec["meas"] = [{"kind": "probs", "qubits": None}]  # 2^10 outcome networks
+    with pytest.raises(NotImplementedError):
+        plan(spec)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_tn_probs_match_oracle(seed):
+    """probs(qubits=...) in the tensor-network mode: one network per outcome
+    (projector products), outcomes ordered with the first listed qubit of the
+    sorted set as the most significant bit, as the reference orders them."""
+    spec = random_spec(seed + 40)
+    n = spec["n"]
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(1, min(3, n) + 1))
+    qs = [int(q) for q in rng.choice(n, k, replace=False)]
+    spec["meas"] = [{"kind": "probs", "qubits": qs}]
+    cc = plan(spec)
+    desc = cc.describe()
+    assert len(desc["nets"]) == 2 ** k
+    prm = flat_params(spec)
+    got = tn_interp.run(desc, prm)
+    want = oracle_out(spec, prm)
+    np.testing.assert_allclose(got, want, atol=1e-12, rtol=1e-12)
+    assert abs(got.sum() - 1.0) < 1e-12
 
 
 @pytest.mark.parametrize("seed", range(4))
