@@ -792,11 +792,15 @@ class GB300Backend:
         cdev = self._cuda_device(params.device)
         Pc = params.to(cdev)
         if self._tn:
-            # one expectation value per measurement: the stacked result is [B, M]
             if not self._requires_grad:
                 with torch.no_grad():
-                    return self._forward(Pc.detach())[0]
-            return GB300TnExecute.apply(self, Pc)
+                    out = self._forward(Pc.detach())[0]
+            else:
+                out = GB300TnExecute.apply(self, Pc)
+            if all(item[0] == "expval" for item in self._prog.layout):
+                return out  # one expectation value per measurement: [B, M]
+            # variances and outcome probabilities from the networks' values
+            return self._assemble(out, torch.empty(out.shape[0], 0))
         if self._sampler is not None:
             self._samples = self._sampler.draw(Pc.detach(), self._ws)
         if not self._requires_grad:
