@@ -233,6 +233,39 @@ def _warp_units(ph, e, R, warp):
     return units
 
 
+def _check_warp_local(desc):
+    marked = total = 0
+    for P in desc["passes"]:
+        e, R = P["e"], P["R"]
+        prev = None
+        for ph in P["phases"]:
+            if ph["type"] != 0:
+                assert not ph.get("wlocal")
+                prev = None
+                continue
+            if prev is not None:
+                total += 1
+            if ph["wlocal"]:
+                assert prev is not None
+                marked += 1
+                for w in range(1 << (len(ph["tid_off"]) - 5)):
+                    assert _warp_units(prev, e, R, w) == _warp_units(ph, e, R, w)
+            prev = ph
+    return marked, total
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+def test_plan_warp_local_transitions_golden_cases(precision):
+    """Warp-local marks stay exact on every golden case (dense phases,
+    controlled and three-qubit gates, small padded states), both sweeps."""
+    for case in CASES:
+        cc = _compile(case, precision)
+        for adjoint in (False, True):
+            if adjoint and not case["params"]:
+                continue
+            _check_warp_local(cc.describe(adjoint=adjoint))
+
+
 @pytest.mark.parametrize("adjoint", [False, True])
 @pytest.mark.parametrize("n,layers", [(14, 3), (20, 10)])
 def test_plan_warp_local_transitions(n, layers, adjoint):
