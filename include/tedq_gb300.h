@@ -138,7 +138,8 @@ typedef struct tedq_program_info {
   int64_t workspace_per_circuit; /* bytes of workspace per circuit of a batch      */
   int32_t jit_state;         /* 0 off, 1 compiling, 2 compiled, 3 loaded, -1 failed  */
   int32_t pad;
-  int64_t reserved[3];
+  int64_t jit_modules_loaded; /* specialised-kernel modules loaded, all devices    */
+  int64_t reserved[2];
 } tedq_program_info_t;
 
 /* ---- library ------------------------------------------------------------ */
@@ -188,9 +189,14 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
  * 1 MiB static device array of this library instead of a caller buffer, for
  * callers that cannot allocate device memory where they run circuits (inside
  * stream capture, allocator callbacks, real-time loops, embedders whose device
- * memory belongs to another runtime).  Batches needing more than 1 MiB of
- * workspace are rejected (TEDQ_ERR_ARG).  The first call on a device looks up
- * the array's address and should come before any stream capture; calls that
+ * memory belongs to another runtime).  The 1 MiB bounds the forward
+ * accumulators: 8 bytes per measured Pauli string and per probability bin of
+ * each circuit, each of the two regions rounded up to 256 bytes; larger
+ * batches are rejected (TEDQ_ERR_ARG).  The first call on a device looks up
+ * the array's address and should come before any stream capture.  The
+ * program's specialised pass kernels are used only if an earlier tedq_run /
+ * tedq_run_adjoint loaded them on this device, otherwise the generic ones run:
+ * this call never waits for a compile and never loads a module.  Calls that
  * overlap on the GPU share the array and race. */
 int32_t tedq_run_noalloc(tedq_program_t* prog, const void* params, int64_t batch, void* psi,
                          void* out_real, const void* init, void* stream);

@@ -91,11 +91,25 @@ def _marginal(prob, n, axes):
     return np.transpose(p, perm).reshape(-1)
 
 
-def metric_tensor(spec, flat_params, numarg):
-    """Block-diagonal metric tensor, float64."""
+def metric_tensor(spec, flat_params, numarg, reference_binding=False):
+    """Block-diagonal metric tensor, float64.
+
+    Each layer circuit's gates take the parameters they were recorded with.
+    ``reference_binding=True`` restates instead what the reference's
+    ``metric_tensor`` does (circuit.py:297-303): it calls the layer circuit
+    with ``parameters[:num_param]`` (the first ``num_param`` flat parameters,
+    ``num_param`` = index of the layer's first selected parameter), and the
+    positional binding (compiled_circuit.py:492-547) hands them to the layer
+    circuit's trainable gates in LAYER order (layers 0..L concatenated,
+    circuit.py:181-182), which differs from gate order when unselected
+    parameters or uneven layers move a gate to an earlier layer; the block is
+    then evaluated at permuted parameters.  A count mismatch raises
+    ``ValueError``, as the reference's binding does; a layer whose first
+    selected parameter is parameter 0 is called with no parameters and keeps
+    the recorded values."""
     n = spec["n"]
     flat = np.asarray(flat_params, dtype=np.float64)
-    layers, obs, factors, _ = layers_of(spec, set(numarg))
+    layers, obs, factors, first = layers_of(spec, set(numarg))
     blocks = []
     for L in sorted(obs):
         gates, sel = [], []
@@ -109,7 +123,15 @@ def metric_tensor(spec, flat_params, numarg):
             gates = gates + dg
             eig.append((vals, qs))
         pspec = {"n": n, "gates": gates, "meas": [{"kind": "probs", "qubits": None}], "init_state": None}
-        prob = run(pspec, torch.tensor(flat[sel], dtype=torch.float64), torch.complex128)
+        vals = flat[sel]
+        if reference_binding and first[L] > 0:
+            # (a call with no parameters keeps the recorded values,
+            # compiled_circuit.py:412-416)
+            vals = flat[:first[L]]
+            if len(vals) != len(sel):
+                raise ValueError(f"Error!!!! number of parameters are not matched!! required {len(sel)} but "
+                                 f"{len(vals)} are given")
+        prob = run(pspec, torch.tensor(vals, dtype=torch.float64), torch.complex128)
         prob = prob.reshape(-1).numpy().real
         k = len(eig)
         cov = np.zeros((k, k))

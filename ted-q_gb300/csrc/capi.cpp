@@ -129,6 +129,19 @@ JitKernels* jit_kernels(tedq_program* h) {
   return k.modules.empty() ? nullptr : &k;
 }
 
+// The specialised kernels of the current device if an earlier call has
+// already loaded them, else nullptr: never waits for the compile and never
+// loads a module (loading allocates device memory for the code).
+JitKernels* jit_kernels_if_loaded(tedq_program* h) {
+  if (!h->jit_on) return nullptr;
+  std::lock_guard<std::mutex> lock(h->jit_mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!h->jit_tried[dev]) return nullptr;
+  JitKernels& k = h->jit_dev[dev];
+  return k.modules.empty() ? nullptr : &k;
+}
+
 int64_t align256(int64_t v) { return (v + 255) & ~int64_t(255); }
 
 struct WsLayout {
@@ -273,6 +286,9 @@ int32_t tedq_program_info(const tedq_program_t* prog, tedq_program_info_t* info)
   info->precision = p.precision;
   info->workspace_per_circuit = ws_layout(p, 1).total;
   info->jit_state = prog->jit_state;
+  int64_t loaded = 0;
+  for (const JitKernels& k : prog->jit_dev) loaded += (int64_t)k.modules.size();
+  info->jit_modules_loaded = loaded;
   return TEDQ_OK;
 }
 
@@ -300,8 +316,17 @@ int64_t tedq_program_describe(const tedq_program_t* prog, int32_t adjoint, char*
   return (int64_t)s.size() + 1;
 }
 
-int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* psi, void* out_real,
-                 const void* init, void* workspace, size_t workspace_bytes, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// The forward of tedq_run.  forward_only: the workspace needs only the
+// forward accumulators (Pauli terms and probability bins, the layout's bytes
+// before the gradient region) and the specialised kernels are used only when
+// already loaded on this device (no compile wait, no module load: the
+// allocation-free entry point).
+int32_t run_forward(tedq_program_t* prog, const void* params, int64_t batch, void* psi, void* out_real,
+                    const void* init, void* workspace, size_t workspace_bytes, void* stream, bool forward_only) {
   if (!prog) return fail(TEDQ_ERR_ARG, "tedq_run: program is null");
   const Program& p = *prog->p;
   if (batch < 0) return fail(TEDQ_ERR_ARG, "tedq_run: negative batch");
@@ -311,7 +336,8 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
   if (p.n_real > 0 && !out_real) return fail(TEDQ_ERR_ARG, "tedq_run: out_real is null");
   const WsLayout L = ws_layout(p, batch);
   const bool need_ws = !p.terms.empty() || p.n_probs_bins > 0;
-  if (need_ws && (!workspace || (int64_t)workspace_bytes < L.total))
+  const int64_t ws_need = forward_only ? L.grad : L.total;
+  if (need_ws && (!workspace || (int64_t)workspace_bytes < ws_need))
     return fail(TEDQ_ERR_ARG, "tedq_run: workspace smaller than tedq_program_workspace_bytes(batch) = " +
                                   std::to_string(L.total));
   if (workspace && (reinterpret_cast<uintptr_t>(workspace) & 255))
@@ -324,7 +350,7 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
     e = timed(prog, 0, 0, s, [&] { return launch_init_state(dbl, p.ns, p.pad, psi, init, batch, s); });
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/init");
   }
-  JitKernels* jk = p.fwd.passes.empty() ? nullptr : jit_kernels(prog);
+  JitKernels* jk = p.fwd.passes.empty() ? nullptr : forward_only ? jit_kernels_if_loaded(prog) : jit_kernels(prog);
   for (size_t i = 0; i < p.fwd.passes.size(); ++i) {
     if (i == 0) {
       PassParams P = p.fwd.passes[0];
@@ -366,6 +392,15 @@ int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* 
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/finalize");
   }
   return TEDQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t tedq_run(tedq_program_t* prog, const void* params, int64_t batch, void* psi, void* out_real,
+                 const void* init, void* workspace, size_t workspace_bytes, void* stream) {
+  return run_forward(prog, params, batch, psi, out_real, init, workspace, workspace_bytes, stream, false);
 }
 
 int32_t tedq_run_adjoint(tedq_program_t* prog, const void* params, int64_t batch, const void* dy_real,
@@ -447,3 +482,16 @@ int32_t tedq_profile_read(tedq_program_t* prog, tedq_profile_t* out) {
 // Records an error message for tedq_last_error from other translation units
 // of this library (C++ linkage, not part of the public ABI).
 int32_t tedq_record_error(int32_t status, const char* msg) { return fail(status, msg ? msg : ""); }
+
+// Forward workspace (bytes before the gradient region of the layout) and the
+// forward that never loads kernels, for the allocation-free entry point
+// (C++ linkage, not part of the public ABI).
+int64_t tedq_forward_workspace_bytes(const tedq_program_t* prog, int64_t batch) {
+  if (!prog || batch < 0) return -1;
+  return ws_layout(*prog->p, batch).grad;
+}
+int32_t tedq_run_forward_loaded_only(tedq_program_t* prog, const void* params, int64_t batch, void* psi,
+                                     void* out_real, const void* init, void* workspace, size_t workspace_bytes,
+                                     void* stream) {
+  return run_forward(prog, params, batch, psi, out_real, init, workspace, workspace_bytes, stream, true);
+}

@@ -54,7 +54,7 @@ class ProgramInfo(ctypes.Structure):
                 ("n_bwd_passes", c_int32), ("n_fwd_phases", c_int32), ("n_bwd_phases", c_int32),
                 ("n_fused_gates", c_int32), ("n_elem_gates", c_int32), ("precision", c_int32),
                 ("workspace_per_circuit", c_int64), ("jit_state", c_int32), ("pad", c_int32),
-                ("reserved", c_int64 * 3)]
+                ("jit_modules_loaded", c_int64), ("reserved", c_int64 * 2)]
 
 
 class Profile(ctypes.Structure):

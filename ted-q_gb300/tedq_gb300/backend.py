@@ -163,8 +163,11 @@ class _Recorded:
                 # <O^2> - <O>^2 from two native expectation values
                 self.layout.append(("var", add_expval(obs), add_expval(obs, square=True)))
             elif kind == "probs" and tn:
-                # the tensor-network mode contracts one network per outcome
-                qs = sorted(set(int(q) for q in (range(self.n) if m.qubits is None else m.qubits)))
+                # the tensor-network mode contracts one network per outcome; the
+                # outcome axes follow the given qubit order, as the reference's
+                # open output indices do (tensor_network.py:1017-1022; its
+                # state-vector mode sorts them, pytorch_backend.py:461-472)
+                qs = list(dict.fromkeys(int(q) for q in (range(self.n) if m.qubits is None else m.qubits)))
                 if len(qs) == 0:
                     raise ValueError("probs(qubits=[]) has no outcome")
                 if len(qs) > self.TN_MAX_PROBS_QUBITS:
@@ -556,7 +559,11 @@ class GB300Backend:
         # tn_mode / use_jdopttn / use_cotengra select the tensor-network path
         # (pytorch_backend.py:242-356); the native planner replaces the external
         # path optimisers, so their objects and hyper_opt are not called
-        self._tn = bool(tn_mode or use_jdopttn or use_cotengra)
+        # a state measurement's network keeps every output index open
+        # (tensor_network.py:953-955): its value is the state vector
+        # U|0...0>, which the state-vector passes compute directly
+        self._tn = bool(tn_mode or use_jdopttn or use_cotengra) and \
+            not any(_kind(m) == "state" for m in circuit.measurements)
         if self._tn:
             self._prog = NativeTnPlan(circuit, self._precision, gemm=kwargs.get("tn_gemm", "auto"),
                                       max_rank=kwargs.get("tn_max_rank", 0), repeats=kwargs.get("tn_repeats", 0),

@@ -143,7 +143,7 @@ class Circuit:
                     obs = [getattr(O, o["name"])(qubits=o["qubits"]) for o in m["obs"]]
                     expval(obs if m.get("list", len(obs) > 1) else obs[0])
                 elif m["kind"] == "probs":
-                    probs(qubits=m["qubits"])
+                    probs(qubits=m["qubits"], after_state=bool(m.get("after_state", False)))
                 else:
                     state()
         return cls(circuit_def, spec["n"])

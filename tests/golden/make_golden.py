@@ -16,65 +16,37 @@ the reference's own circuit API, runs them through the reference's
 * ``param_shift`` gradients for circuits whose output is a 1-D expval list.
 
 The fixtures are consumed by ``tests/`` on machines without the reference.
+
+A second file, ``cases_ext.json``, records three more outputs of the
+reference:
+
+* its tensor-network mode (pytorch_backend.py:242-356, the ``use_jdopttn``
+  branch with ``tn_simplify=False``) on expectation values, ``probs`` with
+  open output indices and ``state``, in complex64 and complex128, with
+  ``OEGreedy`` -- opt_einsum's greedy path and pairwise contraction -- in the
+  place of the external JDtensorPath optimiser, which is not vendored;
+* ``states_after_measurement`` after ``probs(qubits, after_state=True)``
+  (pytorch_backend.py:474-493, tools/helpers.py:22-50);
+* ``Circuit.metric_tensor(Circuit.gen_circuits(numarg), *params)``
+  (circuit.py:166-203, 297-403) on two circuits.
 """
 
-import importlib.abc
-import importlib.machinery
 import json
 import math
 import os
 import sys
-import types
 
 import numpy as np
 import torch
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import refshim  # noqa: E402
+
+REF = sys.argv[1] if len(sys.argv) > 1 else refshim.DEFAULT_PATH
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cases.json")
+OUT_EXT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cases_ext.json")
 
-_STUB_ROOTS = {"jax", "jaxlib", "qiskit", "quafu", "matplotlib", "panel", "IPython",
-               "toolz", "ray", "cotengra", "qiskit_ibm_provider"}
-
-
-class _Stub(types.ModuleType):
-    __path__ = []
-
-    def __getattr__(self, name):
-        if name.startswith("__"):
-            raise AttributeError(name)
-        full = self.__name__ + "." + name
-        if full not in sys.modules:
-            sys.modules[full] = _Stub(full)
-        return sys.modules[full]
-
-    def __call__(self, *a, **k):
-        return _Stub("call")
-
-    def __mro_entries__(self, bases):
-        return (object,)
-
-
-class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
-    def find_spec(self, fullname, path, target=None):
-        if fullname.split(".")[0] in _STUB_ROOTS:
-            return importlib.machinery.ModuleSpec(fullname, self, is_package=True)
-        return None
-
-    def create_module(self, spec):
-        if spec.name == "jax.numpy":
-            return np
-        return _Stub(spec.name)
-
-    def exec_module(self, module):
-        pass
-
-
-sys.meta_path.insert(0, _StubFinder())
-sys.path.insert(0, REF)
-import warnings  # noqa: E402
-
-warnings.filterwarnings("ignore")
-import tedq as qai  # noqa: E402
+qai = refshim.import_reference(REF)
 import tedq.backends.pytorch_backend as pb  # noqa: E402
 
 ONE_Q = ["Hadamard", "PauliX", "PauliY", "PauliZ", "I", "S", "T", "SX"]
@@ -238,29 +210,9 @@ def build_cases():
 
 # --------------------------------------------------------------------------- running
 
-def record(case, rdtype):
-    """Record ``case`` with the reference circuit API; parameters as tensors."""
-    def circuit_def(*_):
-        if case["init_state"] is not None:
-            a = np.asarray(case["init_state"])
-            qai.IintStateVector(a[:, 0] + 1j * a[:, 1], qubits=[])
-        for gg in case["gates"]:
-            cls = getattr(qai, gg["name"])
-            pars = [torch.tensor(p, dtype=rdtype) for p in gg["params"]]
-            op = cls(*pars, qubits=gg["qubits"], trainable_params=gg["trainable"])
-            if gg.get("inv"):
-                op.inverse()
-        out = []
-        for m in case["meas"]:
-            if m["kind"] == "expval":
-                obs = [getattr(qai, o["name"])(qubits=o["qubits"]) for o in m["obs"]]
-                out.append(qai.expval(obs if m["list"] else obs[0]))
-            elif m["kind"] == "probs":
-                out.append(qai.probs(qubits=m["qubits"]))
-            else:
-                out.append(qai.state())
-        return out
-    return qai.Circuit(circuit_def, case["n"])
+def record(case, rdtype, param_shape=()):
+    """Record ``case`` with the reference circuit API (refshim.record_circuit)."""
+    return refshim.record_circuit(qai, case, rdtype, param_shape)
 
 
 def flat_trainable(case):
@@ -327,5 +279,163 @@ def main():
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 
+# --------------------------------------------------------------------------- extended fixtures
+
+class OEGreedy:
+    """Stands in for the external ``JDOptTN`` path optimiser that the
+    reference's ``use_jdopttn`` branch constructs and calls
+    (compiled_circuit.py:388-393, pytorch_backend.py:339): the same
+    constructor and ``contract(arrays, backend=...)``, with opt_einsum's greedy
+    path (the default optimiser of the reference's OEWrapper)."""
+
+    def __init__(self, inputs, size_dict, output=None, **kwargs):
+        import opt_einsum
+        self.eq = ",".join("".join(ix) for ix in inputs) + "->" + "".join(output or [])
+        shapes = [tuple(size_dict[i] for i in ix) for ix in inputs]
+        self.expr = opt_einsum.contract_expression(self.eq, *shapes, optimize="greedy")
+
+    def contract(self, arrays, backend="torch", **kwargs):
+        return self.expr(*arrays, backend=backend)
+
+
+def lattice_case(rows, cols, layers, rng):
+    gates = []
+    for layer in range(layers):
+        for q in range(rows * cols):
+            gates.append(g("Rot", [q], [float(rng.uniform(0, 2 * np.pi)), float(np.arccos(rng.uniform(-1, 1))),
+                                        float(rng.uniform(0, 2 * np.pi))]))
+        par = (layer // 2) % 2
+        if layer % 2 == 0:
+            bonds = [(r * cols + c, r * cols + c + 1) for r in range(rows) for c in range(cols - 1) if c % 2 == par]
+        else:
+            bonds = [(r * cols + c, (r + 1) * cols + c) for r in range(rows - 1) for c in range(cols) if r % 2 == par]
+        for a, b in bonds:
+            gates.append(g("CZ", [a, b]))
+    return gates
+
+
+def random_case(rng, n, depth):
+    gates = []
+    for _ in range(depth):
+        for q in range(n):
+            gates.append(g(ROT1[int(rng.integers(3))], [q], [float(rng.uniform(0, 2 * np.pi))]))
+        for q in range(int(rng.integers(2)), n - 1, 2):
+            gates.append(g(["CNOT", "CZ"][int(rng.integers(2))], [q, q + 1]))
+        gates.append(g("CRY", [int(rng.integers(n - 1)) + 1, 0], [float(rng.uniform(0, 2 * np.pi))]))
+        gates.append(g("Hadamard", [int(rng.integers(n))]))
+    return gates
+
+
+def tn_cases(rng):
+    """Circuits for the reference's tensor-network mode."""
+    cases = []
+    cases.append({"name": "tn_random_n5_expval", "n": 5, "gates": random_case(rng, 5, 3),
+                  "meas": [expval(("PauliZ", [2])), expval(("PauliX", [0]), ("PauliY", [4])),
+                           expval(("PauliZ", [1]), ("PauliZ", [3]))]})
+    cases.append({"name": "tn_lattice_3x3_4layers", "n": 9, "gates": lattice_case(3, 3, 4, rng),
+                  "meas": [expval(("PauliZ", [4]))]})
+    cases.append({"name": "tn_random_n4_probs", "n": 4, "gates": random_case(rng, 4, 2),
+                  "meas": [{"kind": "probs", "qubits": [2, 0]}, {"kind": "probs", "qubits": [1, 3]}]})
+    cases.append({"name": "tn_random_n4_state", "n": 4, "gates": random_case(rng, 4, 2),
+                  "meas": [{"kind": "state"}]})
+    for c in cases:
+        c["init_state"] = None
+    return cases
+
+
+def run_tn_case(case):
+    out = {}
+    for tag, cdt, rdt in (("c64", torch.complex64, torch.float32), ("c128", torch.complex128, torch.float64)):
+        pb.tcomplex = cdt
+        cc = record(case, rdt).compilecircuit(backend="pytorch", use_jdopttn=OEGreedy, tn_simplify=False)
+        res = cc(torch.tensor(flat_trainable(case), dtype=rdt))
+        out[f"out_{tag}"] = to_list(res)
+        out["shape"] = list(res.shape)
+    pb.tcomplex = torch.complex64
+    return out
+
+
+def after_state_case(rng):
+    # a closing RY layer leaves every outcome of the measured qubits possible
+    gates = random_case(rng, 4, 2) + [g("RY", [q], [float(rng.uniform(0.3, 2.8))]) for q in range(4)]
+    return {"name": "after_state_n4", "n": 4, "init_state": None, "gates": gates,
+            "meas": [{"kind": "probs", "qubits": [1, 2], "after_state": True}]}
+
+
+def run_after_state(case):
+    out = {}
+    pb.tcomplex = torch.complex128
+    cc = record(case, torch.float64).compilecircuit(backend="pytorch")
+    res = cc(torch.tensor(flat_trainable(case), dtype=torch.float64))
+    out["out_c128"] = to_list(res)
+    out["shape"] = list(res.shape)
+    after = cc.states_after_measurement
+    out["after_states_c128"] = {k: to_list(torch.stack([torch.as_tensor(x) for x in v]))
+                                for k, v in after.items()}
+    pb.tcomplex = torch.complex64
+    return out
+
+
+def qng_case(rng, name, n, layers, kinds=None):
+    gates = []
+    for layer in range(layers):
+        for q in range(n):
+            kind = ["RX", "RY", "RZ"][int(rng.integers(3))] if kinds is None else kinds[layer][q]
+            gates.append(g(kind, [q], [float(rng.uniform(0, 2 * np.pi))]))
+        for q in range(n - 1):
+            gates.append(g("CNOT", [q, q + 1]))
+    gates.append(g("PhaseShift", [1], [float(rng.uniform(0, 2 * np.pi))]))
+    return {"name": name, "n": n, "init_state": None, "gates": gates, "meas": [expval(("PauliZ", [0]))]}
+
+
+def run_metric_tensor(case, numarg):
+    pb.tcomplex = torch.complex64
+    # metric_tensor runs the first layer's circuit with no call parameters
+    # (parameters[:0], circuit.py:303): its gates keep the recorded values,
+    # which the reference's gate builders need as 1-element tensors
+    circ = record(case, torch.float32, param_shape=(1,))
+    params = [torch.tensor([v], dtype=torch.float32) for v in flat_trainable(case)]
+    mt = circ.metric_tensor(circ.gen_circuits(numarg), *params)
+    return {"metric_tensor": [[float(x) for x in row] for row in mt.detach().double()], "numarg": list(numarg)}
+
+
+def main_ext():
+    rng = np.random.default_rng(20241204)
+    result = {"tn": [], "after_state": [], "metric_tensor": []}
+    for c in tn_cases(rng):
+        rec = run_tn_case(c)
+        entry = dict(c)
+        entry["params"] = flat_trainable(c)
+        entry.update(rec)
+        result["tn"].append(entry)
+        print(f"{c['name']:26s} n={c['n']:2d} gates={len(c['gates']):4d} out={rec['shape']}")
+    c = after_state_case(rng)
+    entry = dict(c)
+    entry["params"] = flat_trainable(c)
+    entry.update(run_after_state(c))
+    result["after_state"].append(entry)
+    print(f"{c['name']:26s} after states {sorted(entry['after_states_c128'])}")
+    # the subset leaves parameter 1 unselected, so its RY on qubit 1 stays in
+    # layer 0 ahead of parameter 0's gate (see run_metric_tensor)
+    for name, n, layers, numarg, kinds in (
+            ("qng_n4_l3_all", 4, 3, None, None),
+            ("qng_n3_l2_subset", 3, 2, [0, 2, 4, 5], [["RY", "RY", "RX"], ["RX", "RY", "RY"]])):
+        c = qng_case(np.random.default_rng(len(name) * 7919), name, n, layers, kinds)
+        P = len(flat_trainable(c))
+        # the last parameter is PhaseShift's: its generator builds the
+        # reference's broken Unitary (qubit.py:1295, 1719), so it stays out
+        na = list(range(P - 1)) if numarg is None else numarg
+        entry = dict(c)
+        entry["params"] = flat_trainable(c)
+        entry.update(run_metric_tensor(c, na))
+        result["metric_tensor"].append(entry)
+        print(f"{name:26s} P={P} metric {len(entry['metric_tensor'])}x{len(entry['metric_tensor'])}")
+    with open(OUT_EXT, "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "reference": "jd-opensource/TeD-Q",
+                   "torch": torch.__version__, **result}, f)
+    print("wrote", OUT_EXT, os.path.getsize(OUT_EXT), "bytes")
+
+
 if __name__ == "__main__":
     main()
+    main_ext()

@@ -81,19 +81,25 @@ def test_tn_slicing_on_device():
 
 
 def test_tn_lattice_6x6_centre_z():
-    """The 6x6, 8-layer workload: complex64 (BF16x9 GEMMs) against complex128 on
-    the device, and complex128 against the float64 plan executor."""
+    """The 6x6, 8-layer workload on the device, complex64 (default GEMM mode)
+    and complex128, for 5 parameter rows, against the independent
+    tensor-network oracle in complex128 (oracle/tn_oracle.py: its own network
+    builder and greedy order), and complex128 against the float64 plan
+    executor."""
+    from oracle import tn_oracle
     spec = lattice_spec(6, 6, 8, seed=0)
     prm = flat_params(spec)
     rng = np.random.default_rng(1)
-    rows = np.stack([prm] + [rng.uniform(0, 2 * np.pi, len(prm)) for _ in range(3)])
+    rows = np.stack([prm] + [rng.uniform(0, 2 * np.pi, len(prm)) for _ in range(4)])
+    want = np.array([tn_oracle.expval(spec, torch.tensor(r, dtype=torch.float64), light_cone=True)[0]
+                     for r in rows])
     c128 = _tn(spec, "c128", requires_grad=False)
     v128 = c128.execute_batch(torch.tensor(rows, dtype=torch.float64, device=DEV)).cpu().numpy()[:, 0]
-    want = tn_interp.run(c128.describe(), prm)[0]
-    assert abs(v128[0] - want) < 1e-12
-    c64 = _tn(spec, "c64", requires_grad=False)
+    np.testing.assert_allclose(v128, want, atol=1e-12, rtol=1e-12)
+    assert abs(v128[0] - tn_interp.run(c128.describe(), prm)[0]) < 1e-12
+    c64 = _tn(spec, "c64", "auto", requires_grad=False)
     v64 = c64.execute_batch(torch.tensor(rows, dtype=torch.float32, device=DEV)).cpu().numpy()[:, 0]
-    np.testing.assert_allclose(v64, v128, atol=1e-5, rtol=1e-5)
+    np.testing.assert_allclose(v64, want, atol=1e-5, rtol=1e-5)
 
 
 def test_tn_graph_replay_follows_parameters():
@@ -168,7 +174,10 @@ def test_tn_non_finite_parameter_gives_nan(gemm):
 
 def test_tn_probs_match_state_vector():
     """probs(qubits=...) in the tensor-network mode (one network per outcome)
-    agrees with the state-vector path, values and parameter-shift gradients."""
+    agrees with the state-vector path, values and parameter-shift gradients.
+    The tensor-network mode orders the outcome axes as the qubits are given
+    (the reference's open output indices, tensor_network.py:1017-1022), the
+    state-vector mode in ascending qubit order (pytorch_backend.py:461-472)."""
     spec = hea_spec(8, 3)
     spec["meas"] = [{"kind": "probs", "qubits": [5, 2]}]
     tn = _tn(spec, "c64", "fp32")
@@ -176,10 +185,10 @@ def test_tn_probs_match_state_vector():
     n = len(flat_params(spec))
     gen = torch.Generator().manual_seed(7)
     P = (torch.rand(3, n, generator=gen) * 6.28).to(DEV)
-    torch.testing.assert_close(tn.execute_batch(P), sv.execute_batch(P), atol=2e-6, rtol=1e-5)
+    torch.testing.assert_close(tn.execute_batch(P), sv.execute_batch(P).transpose(-1, -2), atol=2e-6, rtol=1e-5)
     p1 = P[0].clone().requires_grad_(True)
     p2 = P[0].clone().requires_grad_(True)
     w = torch.arange(4, dtype=torch.float32, device=DEV).reshape(1, 2, 2)
     (tn(p1) * w).sum().backward()
-    (sv(p2) * w).sum().backward()
+    (sv(p2) * w.transpose(-1, -2)).sum().backward()
     torch.testing.assert_close(p1.grad, p2.grad, atol=2e-5, rtol=1e-4)

@@ -193,11 +193,14 @@ def test_tn_capi_rejects_probs_and_bad_input():
     assert L.tedq_tn_plan_destroy(h) == _lib.OK
 
 
-def test_tn_mode_rejects_state_and_wide_probs():
+def test_tn_mode_state_and_wide_probs():
+    """A state measurement's network keeps every output index open
+    (tensor_network.py:953-955): the tensor-network mode evaluates it on the
+    state-vector passes; probs over more than 8 qubits are rejected."""
     spec = random_spec(1)
     spec["meas"] = [{"kind": "state"}]
-    with pytest.raises(NotImplementedError):
-        plan(spec)
+    cc = plan(spec)
+    assert not cc._tn and cc._prog.has_state
     spec = random_spec(2, n=10)
     spec["meas"] = [{"kind": "probs", "qubits": None}]  # 2^10 outcome networks
     with pytest.raises(NotImplementedError):
@@ -207,8 +210,10 @@ def test_tn_mode_rejects_state_and_wide_probs():
 @pytest.mark.parametrize("seed", range(6))
 def test_tn_probs_match_oracle(seed):
     """probs(qubits=...) in the tensor-network mode: one network per outcome
-    (projector products), outcomes ordered with the first listed qubit of the
-    sorted set as the most significant bit, as the reference orders them."""
+    (projector products), outcome axes in the given qubit order with the first
+    listed qubit as the most significant bit, as the reference's open output
+    indices are ordered (tensor_network.py:1017-1022); the state-vector
+    oracle's axes are in ascending qubit order."""
     spec = random_spec(seed + 40)
     n = spec["n"]
     rng = np.random.default_rng(seed)
@@ -220,7 +225,7 @@ def test_tn_probs_match_oracle(seed):
     assert len(desc["nets"]) == 2 ** k
     prm = flat_params(spec)
     got = tn_interp.run(desc, prm)
-    want = oracle_out(spec, prm)
+    want = np.transpose(np.asarray(oracle_out(spec, prm)).reshape([2] * k), np.argsort(np.argsort(qs))).reshape(-1)
     np.testing.assert_allclose(got, want, atol=1e-12, rtol=1e-12)
     assert abs(got.sum() - 1.0) < 1e-12
 
@@ -235,3 +240,18 @@ def test_tn_oracle_matches_state_vector_oracle(seed):
     want = oracle_out(spec, prm)
     np.testing.assert_allclose(tn_oracle.expval(spec, prm), want, atol=1e-12, rtol=1e-12)
     np.testing.assert_allclose(tn_oracle.expval(spec, prm, light_cone=False), want, atol=1e-12, rtol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_tn_lattice_6x6_8layers_matches_tn_oracle(seed):
+    """The full benchmark network (6x6 sites, 8 layers, centre <Z>, 207 gates
+    in the light cone): the planner's exported plan, executed as the device
+    executes it, against the independent tensor-network oracle (its own
+    network builder and greedy order; pinned to the reference's
+    tensor-network mode by tests/golden/cases_ext.json)."""
+    from oracle import tn_oracle
+    spec = lattice_spec(6, 6, 8, seed=seed)
+    prm = flat_params(spec)
+    got = tn_interp.run(plan(spec).describe(), prm)
+    want = tn_oracle.expval(spec, torch.tensor(prm, dtype=torch.float64), light_cone=True)
+    np.testing.assert_allclose(got, want, atol=1e-12, rtol=1e-12)
