@@ -21,6 +21,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -37,6 +38,13 @@ for _p in (ROOT, os.path.join(ROOT, "ted-q_gb300")):
 
 METRIC = "20q VQC value+grad circuits/s"
 UNIT = "circuits/s"
+
+# DRAM bytes per amplitude and pass of the 20-qubit, 10-layer VQC's pass
+# kernels, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch of pass 2 of each sweep at 32 circuits, divided by the
+# 32 x 2^20 amplitudes it streams); the bench scales them to its own launches
+# for the roofline's "traffic" (the algorithmic figures are 16 and 32).
+NCU_DRAM_BYTES_PER_AMP = {"fwd": 14.19, "bwd": 30.17}
 
 
 def vqc_spec(n, layers, seed=0):
@@ -167,6 +175,21 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
+def host_info():
+    """Host cores and CPU model beside every CPU number."""
+    model = platform.processor() or platform.machine()
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"threads": torch.get_num_threads(), "cpu_count": os.cpu_count(), "cpu_model": model,
+            "torch": torch.__version__}
+
+
 def dist_setup(backend="nccl"):
     """Replicas: one process per GPU from torchrun's environment; no data-path
     collective (barriers and a max of the timings only)."""
@@ -250,7 +273,7 @@ def run_reference_arm(a):
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * dt / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": workload_config(a),
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "host": host_info(),
                              "sample": f"{k} circuit(s) of the workload per step, value+grad by back_prop"},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -395,7 +418,7 @@ def run_ours(a):
     e2e = world * B * a.steps / (ms_e2e / 1000.0)
 
     if rank != 0:
-        return 0
+        return None
 
     hbm_peak, peak_kind = read_peaks()
     fam = "bwd" if prof.bwd_ms >= prof.fwd_ms else "fwd"
@@ -405,12 +428,9 @@ def run_ours(a):
     bytes_per_amp = 32 if fam == "bwd" else 16
     per_launch_bytes = bytes_per_amp * amp_passes / max(1, launches)
     achieved = per_launch_bytes / (kms / max(1, launches) / 1000.0) / 1e9
-    # DRAM bytes per amplitude of one pass from an ncu capture of the same
-    # kernels (profiles/sv_pass_kernels_vqc20q_batch32.md: tedq_fwd_2 476.1 MB,
-    # tedq_bwd_2 1012.3 MB for 32 circuits x 2^20 amplitudes), scaled to a launch
     traffic = None
     if a.workload == "vqc" and a.qubits == 20 and a.layers == 10:
-        traffic = {"fwd": 14.19, "bwd": 30.17}[fam] * amp_passes / max(1, launches)
+        traffic = NCU_DRAM_BYTES_PER_AMP[fam] * amp_passes / max(1, launches)
     gpu_launches = prof.fwd_launches + prof.bwd_launches + prof.meas_launches + prof.lam_launches
 
     line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -465,32 +485,104 @@ def run_ours(a):
             line["plain_gpu_per_circuit"] = {"error": str(e)[:200]}
     if not a.no_cpu and a.workload == "mbl24":
         # the reference's back_prop keeps every intermediate state (~380 GiB at
-        # 24 qubits): time its forward pass once
+        # 24 qubits): time its forward pass, on the first a.mbl_cpu_gates gates
+        # (the per-gate tensordot loop costs the same per gate), scaled to all
         import oracle
+        ng = len(spec["gates"])
+        k = min(ng, a.mbl_cpu_gates) if a.mbl_cpu_gates > 0 else ng
+        sub = dict(spec, gates=spec["gates"][:k])
+        Pk = sum(len(g["trainable"]) for g in sub["gates"])
         t0 = time.perf_counter()
-        oracle.run(spec, torch.rand(P, generator=torch.Generator().manual_seed(5)) * 2 * np.pi, torch.complex64)
-        dt = time.perf_counter() - t0
+        oracle.run(sub, torch.rand(Pk, generator=torch.Generator().manual_seed(5)) * 2 * np.pi, torch.complex64)
+        dt = (time.perf_counter() - t0) * ng / k
+        sample = (f"1 circuit, forward only, {dt:.1f} s" if k == ng else
+                  f"forward of the first {k} of {ng} gates of 1 circuit, scaled to all gates: {dt:.1f} s")
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "circuits/s (forward only)",
-                                "cores": torch.get_num_threads(), "kind": "port",
-                                "sample": f"1 circuit, forward only ({dt:.1f} s): back_prop does not fit host memory"}
+                                "cores": torch.get_num_threads(), "kind": "port", "host": host_info(),
+                                "sample": f"{sample}; back_prop does not fit host memory at 24 qubits"}
     elif not a.no_cpu:
         k, _, _ = cpu_sample_size(spec, a.cpu_budget)
         k = min(k, 8 if a.workload == "vqc" else 256)
         rate, dt = cpu_reference(spec, k)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                                "host": host_info(),
                                 "sample": f"{k} circuit(s) of the workload, value+grad by back_prop, {dt:.1f} s"}
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 # ---------------------------------------------------------------- serving stream
+
+def serving_trace(lam, duration, sizes, depths, rng):
+    """Poisson arrivals at ``lam`` req/s for ``duration`` s: (gaps, (n, depth) keys)."""
+    n_req = max(20, int(lam * duration))
+    gaps = rng.exponential(1.0 / lam, n_req)
+    keys = [(sizes[rng.integers(len(sizes))], depths[rng.integers(len(depths))]) for _ in range(n_req)]
+    return gaps, keys
+
+
+def cpu_service_model(sizes, depths, budget_s):
+    """Per-request service time of the reference algorithm on the host (the
+    oracle's per-gate tensordot loop, value + gradient by back_prop,
+    complex64, all host threads) for every (n, depth) of the serving stream.
+    n <= 16: measured at the smallest, middle and largest depth, linear in
+    depth between; n = 20, 24: measured at the smallest depth and scaled
+    linearly in depth (the loop's cost is proportional to the gate count).
+    Returns ({(n, d): seconds}, description)."""
+    import oracle
+    from tedq_gb300.templates import hea_spec
+    gen = torch.Generator().manual_seed(11)
+
+    def one(n, d):
+        spec = hea_spec(n, d)
+        P = sum(len(g["trainable"]) for g in spec["gates"])
+        dy = np.ones(len(spec["meas"]))
+        t0 = time.perf_counter()
+        oracle.value_and_grad(spec, torch.rand(P, generator=gen) * 2 * np.pi, dy, torch.complex64)
+        return time.perf_counter() - t0
+
+    d0, d1, d2 = depths[0], depths[len(depths) // 2], depths[-1]
+    model, t_start = {}, time.perf_counter()
+    one(4, d0)  # warm-up
+    for n in sizes:
+        if n <= 16:
+            pts = {d: one(n, d) for d in (d0, d1, d2)}
+            for d in depths:
+                lo, hi = (d0, d1) if d <= d1 else (d1, d2)
+                model[(n, d)] = pts[lo] + (pts[hi] - pts[lo]) * (d - lo) / (hi - lo)
+        else:
+            t = one(n, d0)
+            for d in depths:
+                model[(n, d)] = t * d / d0
+    desc = (f"reference algorithm per request on the host (oracle port, back_prop, complex64, "
+            f"{torch.get_num_threads()} threads): n <= 16 measured at depths {d0}, {d1}, {d2} and interpolated, "
+            f"n > 16 measured at depth {d0} and scaled by depth; {time.perf_counter() - t_start:.1f} s of "
+            f"measurement; the identical trace replayed through a sequential FIFO server with these times")
+    return model, desc
+
+
+def replay_sequential(gaps, keys, service, sizes):
+    """One request at a time in arrival order (the reference evaluates one
+    circuit per call): throughput and per-bucket latency of the trace."""
+    arrive = np.cumsum(gaps)
+    free_at = 0.0
+    lat = {n: [] for n in sizes}
+    for t, k in zip(arrive, keys):
+        start = max(t, free_at)
+        free_at = start + service[k]
+        lat[k[0]].append(1000.0 * (free_at - t))
+    per = {str(n): {"count": len(v), "p50_ms": float(np.percentile(v, 50)) if v else None,
+                    "p99_ms": float(np.percentile(v, 99)) if v else None} for n, v in lat.items()}
+    return {"throughput_req_s": len(keys) / (free_at - arrive[0] + 1e-12), "per_qubits": per}
+
 
 def run_serving(a):
     """Serving stream: Poisson arrivals of value+grad evaluations of the
     hardware-efficient ansatz, n uniform over {4,8,12,16,20,24}, depth uniform
     in [2, 12], swept over arrival rates; throughput and p50/p99 latency per
     qubit bucket.  Specialised kernels compile in the background while the
-    generic kernels serve."""
+    generic kernels serve.  Size-class lanes: n <= 16 on high-priority streams
+    with reserved memory.  The CPU baseline replays the identical trace through
+    the reference algorithm one request at a time."""
     import threading
     import tedq_gb300 as qai
     from tedq_gb300.serving import Server
@@ -499,18 +591,20 @@ def run_serving(a):
     sizes, depths = [4, 8, 12, 16, 20, 24], list(range(2, 13))
     progs = {(n, d): qai.Circuit.from_spec(hea_spec(n, d)).compilecircuit(backend="gb300", jit=2)
              for n in sizes for d in depths}
-    rng = np.random.default_rng(2024)
     rates = [float(r) for r in a.rates.split(",")]
+    traces = {lam: serving_trace(lam, a.duration, sizes, depths, np.random.default_rng(2024 + int(lam)))
+              for lam in rates}
     results = []
+    t_gpu = time.perf_counter()
     with Server(max_batch=64, max_wait_us=300, memory_budget_bytes=int(a.budget_gb * (1 << 30)),
-                n_streams=8) as srv:
+                n_streams=8, lane_qubits=a.lane_qubits) as srv:
         # warm-up: every program once (loads modules, touches the arena)
         for cc in progs.values():
             srv.wait(srv.submit(cc, np.zeros(cc.num_params, np.float32)), timeout_s=600)
+        rng = np.random.default_rng(7)
         for lam in rates:
-            n_req = max(20, int(lam * a.duration))
-            gaps = rng.exponential(1.0 / lam, n_req)
-            keys = [(sizes[rng.integers(6)], depths[rng.integers(11)]) for _ in range(n_req)]
+            gaps, keys = traces[lam]
+            n_req = len(keys)
             params = [rng.uniform(0, 2 * np.pi, progs[k].num_params).astype(np.float32) for k in keys]
             tickets = [None] * n_req
             t0 = time.perf_counter()
@@ -540,15 +634,24 @@ def run_serving(a):
             results.append({"offered_req_s": lam, "requests": n_req, "throughput_req_s": n_req / wall,
                             "per_qubits": per})
         stats = srv.stats()
+    t_gpu = time.perf_counter() - t_gpu
     top = max(r["throughput_req_s"] for r in results)
-    line = {"metric": "serving value+grad requests/s (mixed n 4-24, HEA depth 2-12)", "value": top,
-            "unit": "requests/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64", "data": "synthetic",
+    line = {"metric": "serving value+grad requests/s (mixed n 4-24, HEA depth 2-12); p50/p99 ms per qubit bucket",
+            "value": top, "unit": "requests/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": {"workload": "serving_stream_poisson", "rates_req_s": rates, "duration_s": a.duration,
-                       "qubits": sizes, "depth": [2, 12], "memory_budget_gb": a.budget_gb, "max_batch": 64},
-            "sweep": results, "server": stats}
-    print(json.dumps(line), flush=True)
-    return 0
+                       "qubits": sizes, "depth": [2, 12], "memory_budget_gb": a.budget_gb, "max_batch": 64,
+                       "n_streams": 8, "lane_qubits": a.lane_qubits if a.lane_qubits else 16},
+            "e2e": {"value": top, "unit": "requests/s",
+                    "what": "requests submitted from host memory, results and gradients returned to host memory"},
+            "sweep": results, "server": stats, "gpu_wall_s": round(t_gpu, 1)}
+    if not a.no_cpu:
+        model, desc = cpu_service_model(sizes, depths, a.cpu_budget)
+        replays = [dict(offered_req_s=lam, **replay_sequential(*traces[lam], model, sizes)) for lam in rates]
+        line["cpu_baseline"] = {"value": replays[-1]["throughput_req_s"], "unit": "requests/s",
+                                "cores": torch.get_num_threads(), "kind": "port", "host": host_info(),
+                                "sample": desc, "sweep": replays}
+    return line
 
 
 # ---------------------------------------------------------------- tensor-network workload
@@ -654,7 +757,7 @@ def run_tn(a):
     e2e = world * B * a.steps / (ms_e2e / 1000.0)
 
     if rank != 0:
-        return 0
+        return None
     # accuracy: complex64 (this GEMM mode) against complex128 on the device and the CPU oracle
     ref = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", tn_mode=True, precision="c128",
                                                       requires_grad=False)
@@ -705,11 +808,49 @@ def run_tn(a):
         rows = params_host[0, : max(1, a.tn_cpu_circuits)].double().numpy()
         rate, dt, vcpu = tn_cpu_rate(spec, rows, np.complex64)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                                "host": host_info(),
                                 "sample": f"{len(rows)} circuit(s), complex64 tensordot contractions, {dt:.1f} s"}
         _, _, v128cpu = tn_cpu_rate(spec, rows[:2], np.complex128)
         line["accuracy"]["max_abs_err_vs_cpu_c128"] = float(np.abs(v64[:2] - v128cpu).max())
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
+
+
+WORKLOAD_SETTINGS = {
+    # per-workload settings of the default run's "workloads" entries (each a
+    # compact line of its own: value, e2e, roofline, cpu_baseline)
+    "small8": {"batch": 4096, "steps": 20, "warmup": 3, "cpu_budget": 5.0},
+    "mbl24": {"batch": 256, "steps": 2, "warmup": 3, "mbl_cpu_gates": 150},
+    "tn": {"batch": 1024, "steps": 10, "warmup": 3, "tn_cpu_circuits": 32},
+    "serving": {"rates": "100,1000", "duration": 2.0},
+}
+ENTRY_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "dtype", "config", "e2e",
+              "gpu_launches", "roofline", "cpu_baseline", "accuracy", "plain_gpu_per_circuit", "sweep", "clocks",
+              "kernels_ms_per_step", "pass_kernels")
+
+
+def run_workloads(a):
+    """The other benchmark configurations, each with its own settings, for the
+    default (N=1) run: 8-qubit HEA, 24-qubit MBL, the tensor-network lattice
+    and the serving stream."""
+    out = {}
+    for name in [w for w in a.workloads.split(",") if w]:
+        b = argparse.Namespace(**vars(a))
+        b.workload = name
+        b.no_plain = name != "small8"
+        for k, v in WORKLOAD_SETTINGS.get(name, {}).items():
+            setattr(b, k, v)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        try:
+            line = run_serving(b) if name == "serving" else run_tn(b) if name == "tn" else run_ours(b)
+            entry = {k: line[k] for k in ENTRY_KEYS if k in line}
+        except Exception as e:  # pragma: no cover - reported, not fatal for the headline
+            entry = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+        entry["wall_s"] = round(time.perf_counter() - t0, 1)
+        out[name] = entry
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -725,12 +866,18 @@ def main():
     ap.add_argument("--jit", type=int, default=0, help="specialised kernels: 0 auto, 1 on, -1 off")
     ap.add_argument("--tile", type=int, default=0, help="forward tile qubits (0 = default)")
     ap.add_argument("--workload", default="vqc", choices=["vqc", "small8", "mbl24", "serving", "tn"])
+    ap.add_argument("--workloads", default="small8,mbl24,tn,serving",
+                    help="with the default vqc workload at N=1: the other configurations to run after it "
+                         "(each reported under 'workloads'); empty = none")
     ap.add_argument("--tn-gemm", default="auto", choices=["bf16x9", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--tn-graphs", type=int, default=0, help="replay each call as a CUDA graph")
     ap.add_argument("--rates", default="100,500,2000,5000")
     ap.add_argument("--duration", type=float, default=2.0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--lane-qubits", type=int, default=0, help="serving lanes: 0 = 16, < 0 = one lane")
+    ap.add_argument("--mbl-cpu-gates", type=int, default=0,
+                    help="mbl24 CPU baseline: time the forward of this many gates and scale (0 = all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -740,10 +887,17 @@ def main():
     if a.impl == "reference":
         return run_reference_arm(a)
     if a.workload == "serving":
-        return run_serving(a)
-    if a.workload == "tn":
-        return run_tn(a)
-    return run_ours(a)
+        line = run_serving(a)
+    elif a.workload == "tn":
+        line = run_tn(a)
+    else:
+        line = run_ours(a)
+    if line is None:  # ranks other than 0
+        return 0
+    if a.workload == "vqc" and line.get("n_gpus", 1) == 1 and a.workloads:
+        line["workloads"] = run_workloads(a)
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 if __name__ == "__main__":

@@ -235,7 +235,10 @@ typedef struct tedq_server_options {
   int64_t memory_budget_bytes; /* device arena for states and buffers                */
   int32_t paused;              /* 1: queue requests but launch nothing until
                                   tedq_server_resume (deterministic batching)       */
-  int32_t pad;
+  int32_t lane_qubits;         /* size-class lanes: states of at most this many
+                                  qubits form the small lane (own high-priority
+                                  streams, half of n_streams, and a reserved 1/8 of
+                                  the budget, at most 8 GiB); 0 = 16, < 0 = one lane */
   int64_t reserved[3];
 } tedq_server_options_t;
 

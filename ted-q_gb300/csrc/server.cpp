@@ -10,7 +10,17 @@
 // batch shrinks until its buffers fit in the free part of the arena, and it is
 // launched on a free stream (H2D, forward, adjoint, D2H, event).  A partially
 // filled batch waits up to max_wait_us for more requests while other batches
-// are in flight.  Batches of different programs overlap on the device.
+// of its lane are in flight.  Batches of different programs overlap on the
+// device.
+//
+// Size-class lanes keep small circuits fast while large ones saturate the
+// GPU: requests of states with at most lane_qubits qubits form the small
+// lane, the rest the large lane.  Each lane has its own streams (the small
+// lane's at the device's highest stream priority, so their CTAs are scheduled
+// ahead of the large lane's as SMs free up), its own share of the memory
+// budget (the small lane's region is reserved, large batches cannot take it)
+// and forms batches from its own queue in arrival order.  A large circuit
+// therefore never holds a stream or memory a small one is waiting for.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +56,12 @@ class Arena {
   void reset(int64_t size) {
     free_.clear();
     if (size > 0) free_[0] = size;
+  }
+  // moves the whole (still free) range to start at `base`
+  void shift(int64_t base) {
+    std::map<int64_t, int64_t> moved;
+    for (auto& kv : free_) moved[kv.first + base] = kv.second;
+    free_.swap(moved);
   }
   bool alloc(int64_t n, int64_t& off) {
     n = align256(n);
@@ -90,6 +106,7 @@ struct Request {
   int64_t ticket = 0;
   tedq_program_t* prog = nullptr;
   ProgInfo info;
+  int lane = 0;  // 0 small, 1 large
   bool grad = false;
   std::vector<char> params, dy, out, gout;
   int state = RQ_QUEUED;
@@ -103,6 +120,7 @@ struct Batch {
   tedq_program_t* prog = nullptr;
   ProgInfo info;
   bool grad = false;
+  int lane = 0;
   int stream = -1;
   cudaEvent_t done = nullptr;
   int64_t dev_off = 0, dev_bytes = 0, host_off = 0, host_bytes = 0;
@@ -117,12 +135,17 @@ struct tedq_server {
   char* dev_arena = nullptr;
   char* host_arena = nullptr;
   int64_t host_size = 0;
-  Arena dA, hA;
+  // per lane: device arena over its region of the budget (offsets relative
+  // to dev_arena), host staging arena
+  Arena dA[2], hA[2];
+  int lane_qubits = 16;  // states of at most this many qubits: small lane
+  int n_lanes = 2;
   std::vector<cudaStream_t> streams;
+  std::vector<int> stream_lane;
   std::vector<bool> stream_busy;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
-  std::deque<std::shared_ptr<Request>> queue;
+  std::deque<std::shared_ptr<Request>> queue[2];
   std::unordered_map<int64_t, std::shared_ptr<Request>> all;
   std::vector<Batch> inflight;
   std::thread worker;
@@ -226,8 +249,8 @@ int32_t launch(tedq_server* S, Batch& b) {
 
 // Forms the next batch from the queue (lock held).  Returns false when nothing
 // should launch now.
-bool form_batch(tedq_server* S, Batch& b, Clock::time_point now) {
-  auto& q = S->queue;
+bool form_batch(tedq_server* S, Batch& b, Clock::time_point now, int lane) {
+  auto& q = S->queue[lane];
   while (!q.empty() && q.front()->state != RQ_QUEUED) q.pop_front();
   if (q.empty()) return false;
   const std::shared_ptr<Request> r0 = q.front();
@@ -237,7 +260,9 @@ bool form_batch(tedq_server* S, Batch& b, Clock::time_point now) {
     cand.push_back(r);
     if ((int)cand.size() == S->opt.max_batch) break;
   }
-  if ((int)cand.size() < S->opt.max_batch && !S->inflight.empty() &&
+  bool lane_busy = false;
+  for (const Batch& f : S->inflight) lane_busy |= f.lane == lane;
+  if ((int)cand.size() < S->opt.max_batch && lane_busy &&
       us_between(r0->t_submit, now) < (double)S->opt.max_wait_us)
     return false;
   int64_t B = (int64_t)cand.size();
@@ -245,15 +270,15 @@ bool form_batch(tedq_server* S, Batch& b, Clock::time_point now) {
   Layout L{};
   for (; B > 0; B /= 2) {
     L = layout(r0->info, r0->prog, B, r0->grad);
-    if (!S->dA.alloc(L.dev_total, doff)) continue;
-    if (!S->hA.alloc(L.host_total, hoff)) {
-      S->dA.release(doff, L.dev_total);
+    if (!S->dA[lane].alloc(L.dev_total, doff)) continue;
+    if (!S->hA[lane].alloc(L.host_total, hoff)) {
+      S->dA[lane].release(doff, L.dev_total);
       continue;
     }
     break;
   }
   if (B == 0) {
-    if (S->inflight.empty()) {  // can never fit: fail the request
+    if (!lane_busy) {  // can never fit: fail the request
       r0->state = RQ_DONE;
       r0->status = TEDQ_ERR_OOM;
       r0->t_done = now;
@@ -266,6 +291,7 @@ bool form_batch(tedq_server* S, Batch& b, Clock::time_point now) {
   b.prog = r0->prog;
   b.info = r0->info;
   b.grad = r0->grad;
+  b.lane = lane;
   b.dev_off = doff;
   b.dev_bytes = L.dev_total;
   b.host_off = hoff;
@@ -312,8 +338,8 @@ bool retire(tedq_server* S) {
       else S->stats.failed++;
     }
     cudaEventDestroy(b.done);
-    S->dA.release(b.dev_off, b.dev_bytes);
-    S->hA.release(b.host_off, b.host_bytes);
+    S->dA[b.lane].release(b.dev_off, b.dev_bytes);
+    S->hA[b.lane].release(b.host_off, b.host_bytes);
     S->stats.in_flight_bytes -= b.dev_bytes;
     S->stream_busy[b.stream] = false;
     S->inflight.erase(S->inflight.begin() + i);
@@ -323,14 +349,16 @@ bool retire(tedq_server* S) {
 }
 
 void fail_queued(tedq_server* S, int32_t status) {
-  for (auto& r : S->queue)
-    if (r->state == RQ_QUEUED) {
-      r->state = RQ_DONE;
-      r->status = status;
-      r->t_done = Clock::now();
-      S->stats.failed++;
-    }
-  S->queue.clear();
+  for (auto& q : S->queue) {
+    for (auto& r : q)
+      if (r->state == RQ_QUEUED) {
+        r->state = RQ_DONE;
+        r->status = status;
+        r->t_done = Clock::now();
+        S->stats.failed++;
+      }
+    q.clear();
+  }
   S->cv_done.notify_all();
 }
 
@@ -350,7 +378,7 @@ void worker_main(tedq_server* S) {
         Batch b;
         b.stream = (int)si;
         b.done = nullptr;
-        if (!form_batch(S, b, Clock::now())) break;
+        if (!form_batch(S, b, Clock::now(), S->stream_lane[si])) continue;
         S->stream_busy[si] = true;
         cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
         lk.unlock();
@@ -399,12 +427,33 @@ int32_t tedq_server_create(const tedq_server_options_t* opts, tedq_server_t** ou
     cudaSetDevice(prev);
     return tedq_record_error(TEDQ_ERR_OOM, "tedq_server_create: pinned host staging cannot be allocated");
   }
-  S->dA.reset(S->opt.memory_budget_bytes);
-  S->hA.reset(S->host_size);
+  // lanes: lane_qubits < 0 or a single stream puts every request in one lane
+  S->lane_qubits = S->opt.lane_qubits == 0 ? 16 : S->opt.lane_qubits;
+  S->n_lanes = (S->lane_qubits < 0 || S->opt.n_streams < 2) ? 1 : 2;
+  if (S->n_lanes == 1) {
+    S->dA[1].reset(S->opt.memory_budget_bytes);  // everything in the large lane
+    S->hA[1].reset(S->host_size);
+  } else {
+    // the small lane's reserve: 1/8 of the budget, at most 8 GiB (a batch of
+    // 256 value+grad requests of 16 qubits needs 256 MiB of states)
+    const int64_t small = std::min<int64_t>(int64_t(8) << 30, align256(S->opt.memory_budget_bytes / 8));
+    S->dA[0].reset(small);
+    S->dA[1].reset(S->opt.memory_budget_bytes - small);
+    S->dA[1].shift(small);
+    const int64_t hsmall = align256(S->host_size / 4);
+    S->hA[0].reset(hsmall);
+    S->hA[1].reset(S->host_size - hsmall);
+    S->hA[1].shift(hsmall);
+  }
+  int prio_low = 0, prio_high = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  const int n_small = S->n_lanes == 1 ? 0 : std::max(1, S->opt.n_streams / 2);
   for (int i = 0; i < S->opt.n_streams; ++i) {
+    const int lane = i < n_small ? 0 : 1;
     cudaStream_t st;
-    cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lane == 0 ? prio_high : prio_low);
     S->streams.push_back(st);
+    S->stream_lane.push_back(lane);
     S->stream_busy.push_back(false);
   }
   cudaSetDevice(prev);
@@ -442,6 +491,7 @@ int32_t tedq_server_submit(tedq_server_t* S, tedq_program_t* prog, const void* p
   if (r->info.ns == 0) return tedq_record_error(TEDQ_ERR_ARG, "tedq_server_submit: invalid program");
   if (r->info.n_params > 0 && !params) return tedq_record_error(TEDQ_ERR_ARG, "tedq_server_submit: params is null");
   r->grad = with_grad != 0;
+  r->lane = (S->n_lanes == 2 && r->info.ns <= S->lane_qubits) ? 0 : 1;
   const size_t pbytes = (size_t)r->info.n_params * r->info.rbytes, rbytes = (size_t)r->info.n_real * r->info.rbytes;
   if (pbytes) r->params.assign((const char*)params, (const char*)params + pbytes);
   if (dy && rbytes) r->dy.assign((const char*)dy, (const char*)dy + rbytes);
@@ -451,7 +501,7 @@ int32_t tedq_server_submit(tedq_server_t* S, tedq_program_t* prog, const void* p
     if (S->stop) return tedq_record_error(TEDQ_ERR_STATE, "tedq_server_submit: server is stopping");
     r->ticket = S->next_ticket++;
     S->all[r->ticket] = r;
-    S->queue.push_back(r);
+    S->queue[r->lane].push_back(r);
     S->stats.submitted++;
     *ticket = r->ticket;
   }

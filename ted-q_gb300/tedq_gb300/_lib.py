@@ -65,7 +65,8 @@ class Profile(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("device", c_int32), ("n_streams", c_int32), ("max_batch", c_int32), ("max_wait_us", c_int32),
-                ("memory_budget_bytes", c_int64), ("paused", c_int32), ("pad", c_int32), ("reserved", c_int64 * 3)]
+                ("memory_budget_bytes", c_int64), ("paused", c_int32), ("lane_qubits", c_int32),
+                ("reserved", c_int64 * 3)]
 
 
 class RequestResult(ctypes.Structure):

@@ -25,12 +25,16 @@ class RequestError(RuntimeError):
 
 class Server:
     def __init__(self, device=0, n_streams=4, max_batch=256, max_wait_us=200, memory_budget_bytes=1 << 30,
-                 paused=False):
+                 paused=False, lane_qubits=0):
+        """``lane_qubits``: states of at most this many qubits are served in
+        the small lane (own high-priority streams and a reserved part of the
+        budget); 0 = 16, a negative value = one lane for every request."""
         L = _lib.lib()
         o = _lib.ServerOptions()
         o.device, o.n_streams, o.max_batch, o.max_wait_us = device, n_streams, max_batch, max_wait_us
         o.memory_budget_bytes = int(memory_budget_bytes)
         o.paused = 1 if paused else 0
+        o.lane_qubits = int(lane_qubits)
         h = ctypes.c_void_p()
         _lib.check(L.tedq_server_create(ctypes.byref(o), ctypes.byref(h)), "tedq_server_create")
         self._h = h

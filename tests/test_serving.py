@@ -116,3 +116,27 @@ def test_kernel_limits_shared_across_threads():
     out = big.execute_batch(torch.zeros(2, big.num_params, device=DEV))
     torch.cuda.synchronize()
     assert torch.allclose(out, torch.ones_like(out))
+
+
+def test_small_request_not_blocked_by_large_batches():
+    """Size-class lanes: a 4-qubit request submitted while 24-qubit batches
+    hold the large lane's streams and memory completes before those batches
+    do (its own high-priority stream and reserved memory), with the result it
+    has alone."""
+    big, small = _compile(24, 8), _compile(4, 2)
+    rng = np.random.default_rng(3)
+    with Server(n_streams=4, max_batch=32, max_wait_us=100, memory_budget_bytes=16 << 30) as srv:
+        for cc in (big, small):  # warm-up: compile and load the kernels
+            srv.wait(srv.submit(cc, np.zeros(cc.num_params, dtype=np.float32)), timeout_s=300)
+        bigs = [srv.submit(big, rng.uniform(0, 2 * np.pi, big.num_params).astype(np.float32)) for _ in range(64)]
+        time.sleep(0.02)
+        p = rng.uniform(0, 2 * np.pi, small.num_params).astype(np.float32)
+        out, grad, info = srv.wait(srv.submit(small, p), timeout_s=60)
+        with pytest.raises(TimeoutError):  # the large batches are still running
+            srv.wait(bigs[-1], timeout_s=0)
+        want_out, want_grad = _alone(small, p)
+        np.testing.assert_allclose(out, want_out, atol=1e-5, rtol=1e-5)
+        np.testing.assert_allclose(grad, want_grad, atol=1e-5, rtol=1e-5)
+        for t in bigs:
+            srv.wait(t, timeout_s=300)
+        assert srv.stats()["completed"] == 64 + 3
