@@ -769,16 +769,21 @@ def run_tn(a):
             bf16 = float(json.load(f)["bf16_tflops"])
     except Exception:
         bf16, peak_kind = 1900.0, "fallback"
-    if a.tn_gemm in ("bf16x9", "auto"):
-        peak = bf16 / 9.0
-        peak_kind += " bf16 dense / 9 (each FP32 product is 9 BF16 tensor-core products)"
+    if a.tn_gemm in ("tc32", "auto"):
+        peak = bf16 / 2.0 / 3.0
+        peak_kind += (" bf16 dense / 2 (TF32 rate) / 3 (each FP32-accurate product is three TF32 "
+                      "tensor-core products)")
     elif a.tn_gemm == "tf32":
         peak = bf16 / 2.0
         peak_kind += " bf16 dense / 2 (TF32 rate)"
     else:
         peak = None
         peak_kind = "FP32 SIMT (no tensor-core peak)"
-    achieved = prof.gemm_flops / (prof.gemm_ms / 1000.0) / 1e12 if prof.gemm_ms else 0.0
+    # the dominant kernel: the tensor-core GEMMs when they run, else every
+    # contraction launch
+    tc = prof.tc_ms > 0
+    achieved = (prof.tc_flops / (prof.tc_ms / 1000.0) / 1e12 if tc else
+                prof.gemm_flops / (prof.gemm_ms / 1000.0) / 1e12 if prof.gemm_ms else 0.0)
     per_call = prof.leaf_launches + prof.gather_launches + prof.gemm_launches + prof.root_launches
     line = {"metric": TN_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -794,10 +799,14 @@ def run_tn(a):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": B * P * 4, "d2h_bytes_per_step": B * 4},
             "gpu_launches": int(per_call),
             "roofline": {"bound": "tensor",
-                         "kernel": "contractions: fused in-place kernels (small) + cuBLAS strided-batched GEMMs "
-                                   "(4M real embedding; BF16x9 tensor cores for >= 2^20 flops per circuit)",
+                         "kernel": ("tn_gemm_tc_kernel (tcgen05 kind::tf32, 3xTF32 split; 4M real embedding)" if tc
+                                    else "contractions: level launches + FMA GEMMs"),
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if peak else None, "traffic": None, "peak_kind": peak_kind,
+                         "tc_gemm_launches_per_step": prof.tc_launches / a.steps,
+                         "tc_gemm_ms_per_step": prof.tc_ms / a.steps,
+                         "contractions_tflops": (prof.gemm_flops / (prof.gemm_ms / 1000.0) / 1e12
+                                                 if prof.gemm_ms else 0.0),
                          "gemm_ms_per_step": prof.gemm_ms / a.steps, "gather_ms_per_step": prof.gather_ms / a.steps,
                          "gather_gbs": prof.gather_bytes / (prof.gather_ms / 1000.0) / 1e9 if prof.gather_ms else 0,
                          "leaf_ms_per_step": prof.leaf_ms / a.steps, "root_ms_per_step": prof.root_ms / a.steps,
@@ -869,7 +878,7 @@ def main():
     ap.add_argument("--workloads", default="small8,mbl24,tn,serving",
                     help="with the default vqc workload at N=1: the other configurations to run after it "
                          "(each reported under 'workloads'); empty = none")
-    ap.add_argument("--tn-gemm", default="auto", choices=["bf16x9", "tf32", "fp32", "auto"])
+    ap.add_argument("--tn-gemm", default="auto", choices=["tc32", "tf32", "fp32", "auto"])
     ap.add_argument("--tn-cpu-circuits", type=int, default=64)
     ap.add_argument("--tn-graphs", type=int, default=0, help="replay each call as a CUDA graph")
     ap.add_argument("--rates", default="100,500,2000,5000")

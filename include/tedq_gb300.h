@@ -301,21 +301,27 @@ int32_t tedq_profile_read(tedq_program_t* prog, tedq_profile_t* out);
  * compiled_circuit.py:388-393) and torch einsum.  One network per
  * measurement, reduced to the backward light cone of its observable, ordered
  * by randomised greedy search and sliced until every intermediate fits
- * 2^max_rank entries.  Each pairwise contraction runs as two bit-permutation
+ * 2^max_rank entries.  Small pairwise contractions run in level launches
+ * that read their operands in place; each large one as two bit-permutation
  * gathers into planar real operands and one real GEMM on the tensor cores
  * (4M decomposition: [Re A; Im A] x [Re B, Im B]), batched over the circuits
  * of a call.  Expectation values of tensor products of observable factors
- * only (the reference's TN mode also returns probs/state, :1017-1022). */
+ * (the Python layer builds probs(qubits=...) from projector products; a
+ * state measurement runs on the state-vector passes). */
 typedef struct tedq_tn_plan tedq_tn_plan_t;
 
-/* GEMM arithmetic of the complex64 mode (complex128 uses FP64 GEMMs). */
+/* GEMM arithmetic of the complex64 mode (complex128 uses FP64 FMA GEMMs).
+ * All GEMMs are kernels of this library: tcgen05 tensor-core MMAs (TF32
+ * operands staged by TMA, FP32 accumulators in tensor memory) or FMA. */
 enum {
-  TEDQ_TN_GEMM_FP32 = 0,    /* FP32 (default)                                 */
-  TEDQ_TN_GEMM_BF16X9 = 1,  /* FP32 accuracy from BF16 tensor-core products
-                               (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9)    */
+  TEDQ_TN_GEMM_FP32 = 0,    /* FP32 FMA                                       */
+  TEDQ_TN_GEMM_TC32 = 1,    /* FP32 accuracy on the tensor cores: each operand
+                               split into two TF32 parts, three products
+                               (hi*hi + hi*lo + lo*hi)                        */
   TEDQ_TN_GEMM_TF32 = 2,    /* one TF32 product per term (~1e-3 relative)     */
-  TEDQ_TN_GEMM_AUTO = 3     /* BF16x9 for the large contractions (at least 2^20
-                               flops per circuit), FP32 for the rest          */
+  TEDQ_TN_GEMM_AUTO = 3     /* TC32 for the contractions of at least 2^16
+                               flops per circuit whose shape fills the
+                               tensor-core tiles, FP32 FMA for the rest       */
 };
 
 typedef struct tedq_tn_options {
@@ -367,7 +373,11 @@ int32_t tedq_tn_contract(tedq_tn_plan_t* plan, const void* params, int64_t batch
  * enabled, calls run without graphs and record CUDA events around every launch
  * on the launch stream; read sums the durations per launch family since the
  * last read, with the algorithmic work of the launches (gather bytes: source
- * read + planar operand write; GEMM flops: 2 per real multiply-add). */
+ * read + planar operand write; contraction flops: 2 per real multiply-add).
+ * gemm_* covers every contraction launch (level launches, FMA and tensor-core
+ * GEMMs), tc_* the tensor-core GEMMs alone.  gemm_error is the device error
+ * word of the tensor-core GEMMs: nonzero when one gave up a bounded wait (the
+ * read then returns TEDQ_ERR_TIMEOUT and the calls' results are NaN). */
 typedef struct tedq_tn_profile {
   int64_t leaf_launches;
   double leaf_ms;
@@ -379,11 +389,31 @@ typedef struct tedq_tn_profile {
   double gemm_flops;
   int64_t root_launches;
   double root_ms;
-  int64_t reserved[4];
+  int64_t tc_launches;
+  double tc_ms;
+  double tc_flops;
+  int32_t gemm_error;
+  int32_t pad;
 } tedq_tn_profile_t;
 
 int32_t tedq_tn_profile_enable(tedq_tn_plan_t* plan, int32_t on);
 int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out);
+
+/* The batched real GEMM that tedq_tn_contract runs for each large pairwise
+ * contraction, on caller buffers (no counterpart in the reference, whose
+ * contractions are torch einsum calls; exposed for testing and for callers
+ * with operands of their own):
+ *   C[b](i, j) = sum_k A[b](i, k) B[b](j, k),   b < nbatch (<= 65535),
+ * A [mr][kr] and B [nr][kr] row-major (K contiguous), C column-major (C[j*mr+i]);
+ * sa, sb, sc: elements between batch entries (0: operand shared by all).
+ * precision TEDQ_PREC_C64: float data, mode TEDQ_TN_GEMM_* (TC32 / TF32
+ * return TEDQ_ERR_UNSUPPORTED where the tensor-core kernel does not apply:
+ * kr a multiple of 4 and >= 8, the larger of mr, nr >= 32, the smaller >= 8,
+ * 16-byte aligned A and B; AUTO then uses FMA); TEDQ_PREC_C128: double data,
+ * FP64 FMA.  err_word: a device int32 that the tensor-core kernel sets when
+ * one of its bounded waits gives up (required for TC32 / TF32 / AUTO). */
+int32_t tedq_tn_gemm(int32_t precision, int32_t gemm, const void* a, const void* b, void* c, int64_t mr, int64_t nr,
+                     int64_t kr, int64_t sa, int64_t sb, int64_t sc, int64_t nbatch, int32_t* err_word, void* stream);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(PKG_ROOT, "_build")
 OUT = os.path.join(PKG_ROOT, "tedq_gb300", "libtedq_gb300.so")
 
-CU_SOURCES = ["sv_kernels.cu", "noalloc.cu", "tn_kernels.cu"]
+CU_SOURCES = ["sv_kernels.cu", "noalloc.cu", "tn_kernels.cu", "tn_gemm.cu"]
 CPP_SOURCES = ["sv_program.cpp", "capi.cpp", "sv_jit.cpp", "server.cpp", "tn_plan.cpp", "tn_capi.cpp"]
 # headers compiled again at run time by NVRTC for the per-circuit kernels
 JIT_HEADERS = ["sv_plan.h", "sv_device.cuh"]

@@ -6,13 +6,12 @@
 // per call (compiled_circuit.py:442-467, pytorch_backend.py:524-546) and hands
 // it to the path object's contract().  Here the plan is built once; a call
 // builds the parameter-dependent gate tensors of the whole batch on the device
-// and runs the planned pairwise contractions, each as one gather launch and
-// one strided-batched real GEMM over the batch.  cuBLAS is opened at run time
-// (no link-time dependency), and a CUDA graph of a call's launches can be
-// replayed when the same buffers are used again.
+// and runs the planned pairwise contractions: the small ones in level
+// launches that read their operands in place, the large ones as one gather
+// launch and one batched real GEMM of this library (tn_gemm.cu: tcgen05
+// tensor cores, 3xTF32 for FP32 accuracy) over the batch.  A CUDA graph of a
+// call's launches can be replayed when the same buffers are used again.
 #include <cuda_runtime.h>
-#include <cublas_api.h>  // types and enums; the library is opened with dlopen
-#include <dlfcn.h>
 
 #include <algorithm>
 #include <cmath>
@@ -26,6 +25,7 @@
 
 #include "sv_program.h"
 #include "tedq_gb300.h"
+#include "tn_gemm.cuh"
 #include "tn_kernels.cuh"
 #include "tn_plan.h"
 
@@ -34,64 +34,6 @@ using namespace tedq;
 int32_t tedq_record_error(int32_t status, const char* msg);
 
 namespace {
-
-// ------------------------------------------------------------------ cuBLAS
-
-struct Blas {
-  bool ok = false;
-  std::string why;
-  cublasStatus_t (*create)(cublasHandle_t*) = nullptr;
-  cublasStatus_t (*destroy)(cublasHandle_t) = nullptr;
-  cublasStatus_t (*set_stream)(cublasHandle_t, cudaStream_t) = nullptr;
-  cublasStatus_t (*set_workspace)(cublasHandle_t, void*, size_t) = nullptr;
-  cublasStatus_t (*set_emulation)(cublasHandle_t, cublasEmulationStrategy_t) = nullptr;
-  // optional: special-value handling of emulated GEMMs
-  cublasStatus_t (*set_special)(cublasHandle_t, cudaEmulationSpecialValuesSupport) = nullptr;
-  const char* (*status_string)(cublasStatus_t) = nullptr;
-  cublasStatus_t (*gemm)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int, int, int, const void*,
-                         const void*, cudaDataType, int, long long, const void*, cudaDataType, int, long long,
-                         const void*, void*, cudaDataType, int, long long, int, cublasComputeType_t,
-                         cublasGemmAlgo_t) = nullptr;
-};
-
-Blas load_blas() {
-  Blas b;
-  std::vector<std::string> cands = {"libcublas.so.13", "libcublas.so"};
-  for (const char* env : {"CUDA_HOME", "CUDA_PATH"})
-    if (const char* d = getenv(env)) cands.push_back(std::string(d) + "/lib64/libcublas.so.13");
-  cands.push_back("/usr/local/cuda/lib64/libcublas.so.13");
-  void* h = nullptr;
-  for (auto& c : cands)
-    if ((h = dlopen(c.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
-  if (!h) {
-    b.why = "libcublas.so.13 not found";
-    return b;
-  }
-#define TEDQ_SYM(field, name)                                  \
-  b.field = reinterpret_cast<decltype(b.field)>(dlsym(h, name)); \
-  if (!b.field) {                                              \
-    b.why = std::string("missing symbol ") + name;             \
-    return b;                                                  \
-  }
-  TEDQ_SYM(create, "cublasCreate_v2")
-  TEDQ_SYM(destroy, "cublasDestroy_v2")
-  TEDQ_SYM(set_stream, "cublasSetStream_v2")
-  TEDQ_SYM(set_workspace, "cublasSetWorkspace_v2")
-  TEDQ_SYM(set_emulation, "cublasSetEmulationStrategy")
-  TEDQ_SYM(status_string, "cublasGetStatusString")
-  TEDQ_SYM(gemm, "cublasGemmStridedBatchedEx")
-#undef TEDQ_SYM
-  b.set_special = reinterpret_cast<decltype(b.set_special)>(dlsym(h, "cublasSetEmulationSpecialValuesSupport"));
-  b.ok = true;
-  return b;
-}
-
-Blas& blas() {
-  static Blas b = load_blas();
-  return b;
-}
-
-constexpr size_t kBlasWorkspace = 32ull << 20;
 
 inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -109,7 +51,7 @@ struct TnLevelRun {
 
 struct TnDevice {
   bool ready = false;
-  cublasHandle_t handle = nullptr;
+  int* err = nullptr;           // error word of the tensor-core GEMMs (bounded waits)
   void* consts = nullptr;       // constants of all networks (plan precision)
   TnLeafDesc* desc = nullptr;   // batched-leaf descriptors of all networks
   // graph of the last call, replayed while its arguments repeat
@@ -139,7 +81,7 @@ struct tedq_tn_plan {
   // kernel timing (tedq_tn_profile_*)
   struct Ev {
     cudaEvent_t a, b;
-    int family;  // 0 leaf, 1 gather, 2 gemm, 3 root
+    int family;  // 0 leaf, 1 gather, 2 contraction (FMA), 3 root, 4 tensor-core GEMM
     double work;
   };
   bool profiling = false;
@@ -152,17 +94,16 @@ namespace {
 int64_t elem_bytes(const tedq_tn_plan* p) { return p->precision == TEDQ_PREC_C128 ? 8 : 4; }
 
 struct Layout {
-  size_t acc, blas_ws, leaves, arena_b, arena_u, scratch, total;
+  size_t acc, leaves, arena_b, arena_u, scratch, total;
 };
 
-// acc (FP64 sums) | cuBLAS workspace | per network (reused): batched leaves,
-// batched arena, unbatched arena, GEMM operand scratch
+// acc (FP64 sums) | per network (reused): batched leaves, batched arena,
+// unbatched arena, GEMM operand scratch
 Layout layout(const tedq_tn_plan* p, int64_t batch) {
   const size_t es = (size_t)elem_bytes(p);
   Layout L{};
   L.acc = 0;
-  L.blas_ws = align256((size_t)batch * p->nets.size() * sizeof(double));
-  size_t region = L.blas_ws + kBlasWorkspace;
+  size_t region = align256((size_t)batch * p->nets.size() * sizeof(double));
   size_t most = 0, mleaves = 0, mab = 0, mau = 0;
   for (const TnNet& n : p->nets) {
     size_t lv = align256(2 * (size_t)n.batched_leaf_elems * batch * es);
@@ -188,9 +129,6 @@ int32_t cuda_fail(const char* where, cudaError_t e) {
   return fail(TEDQ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
-int32_t blas_fail(const char* where, cublasStatus_t st) {
-  return fail(TEDQ_ERR_CUDA, std::string(where) + ": " + blas().status_string(st));
-}
 
 #define TEDQ_CUDA(where, expr)                    \
   do {                                            \
@@ -198,28 +136,13 @@ int32_t blas_fail(const char* where, cublasStatus_t st) {
     if (e_ != cudaSuccess) return cuda_fail(where, e_); \
   } while (0)
 
-// Device-resident constants, descriptors and the cuBLAS handle (first use).
+// Device-resident constants, descriptors and the error word (first use).
 int32_t ensure_device(tedq_tn_plan* p, int dev) {
   TnDevice& D = p->dev[dev];
   if (D.ready) return TEDQ_OK;
-  Blas& B = blas();
-  if (!B.ok) return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_contract: cuBLAS unavailable: " + B.why);
-  if (!D.handle) {
-    cublasStatus_t st = B.create(&D.handle);
-    if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasCreate", st);
-    if (p->precision == TEDQ_PREC_C64 && (p->gemm == TEDQ_TN_GEMM_BF16X9 || p->gemm == TEDQ_TN_GEMM_AUTO)) {
-      st = B.set_emulation(D.handle, CUBLAS_EMULATION_STRATEGY_EAGER);
-      if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetEmulationStrategy", st);
-      // operands are finite whenever the parameters are (gate entries and
-      // their products): no scan and patch passes for infinities and NaNs.
-      // Circuits with a non-finite parameter are flagged by the gate-tensor
-      // kernel and return NaN from the root kernel instead.
-      if (B.set_special) {
-        st = B.set_special(D.handle, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE);
-        if (st != CUBLAS_STATUS_SUCCESS)
-          return blas_fail("tedq_tn_contract: cublasSetEmulationSpecialValuesSupport", st);
-      }
-    }
+  if (!D.err) {
+    TEDQ_CUDA("tedq_tn_contract: cudaMalloc", cudaMalloc(&D.err, sizeof(int)));
+    TEDQ_CUDA("tedq_tn_contract: cudaMemset", cudaMemset(D.err, 0, sizeof(int)));
   }
   const size_t es = (size_t)elem_bytes(p);
   if (!D.consts) {
@@ -379,29 +302,16 @@ template <typename real>
 int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch, real* out, char* ws,
                 cudaStream_t s) {
   const Layout L = layout(p, batch);
-  Blas& bl = blas();
-  cublasStatus_t st = bl.set_stream(D.handle, s);
-  if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetStream", st);
-  st = bl.set_workspace(D.handle, ws + L.blas_ws, kBlasWorkspace);
-  if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasSetWorkspace", st);
   double* acc = reinterpret_cast<double*>(ws + L.acc);
   real* leaves = reinterpret_cast<real*>(ws + L.leaves);
   real* arena_b = reinterpret_cast<real*>(ws + L.arena_b);
   real* arena_u = reinterpret_cast<real*>(ws + L.arena_u);
   real* scratch = reinterpret_cast<real*>(ws + L.scratch);
   const bool dbl = sizeof(real) == 8;
-  const cudaDataType dt = dbl ? CUDA_R_64F : CUDA_R_32F;
-  cublasComputeType_t ct = CUBLAS_COMPUTE_64F;
-  if (!dbl)
-    ct = p->gemm == TEDQ_TN_GEMM_TF32   ? CUBLAS_COMPUTE_32F_FAST_TF32
-         : p->gemm == TEDQ_TN_GEMM_BF16X9 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
-                                          : CUBLAS_COMPUTE_32F;
-  // AUTO: BF16x9 on the tensor cores for contractions of at least 2^auto_log2
-  // real flops per circuit, FP32 below (measured on the 6x6 lattice: 2^20 to
-  // 2^22 best once the emulation runs without special-value passes)
-  int auto_log2 = 20;
+  // AUTO: the FP32-accurate tensor-core GEMM for contractions of at least
+  // 2^auto_log2 real flops per circuit, FMA below
+  int auto_log2 = 16;
   if (const char* env = getenv("TEDQ_GB300_TN_AUTO_LOG2")) auto_log2 = atoi(env);
-  const real one = 1, zero = 0;
   const int n_meas = (int)p->nets.size();
   for (int m = 0; m < n_meas; ++m) {
     const TnNet& net = p->nets[m];
@@ -552,16 +462,30 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
         // real embedding: [Re A, Im A] x [[Re B, Im B], [-Im B, Re B]] (B doubled) or
         // [[Re A, -Im A], [Im A, Re A]] x [Re B; Im B] (A doubled); K is doubled either way
         const long long mr = stp.double_a ? 2 * M : M, nr = stp.double_a ? N : 2 * N;
-        const long long sa = A.op[0].nb > 1 ? mr * 2 * K : 0, sb = A.op[1].nb > 1 ? nr * 2 * K : 0;
-        const cublasComputeType_t cts =
-            (!dbl && p->gemm == TEDQ_TN_GEMM_AUTO && 8.0 * M * N * K >= std::ldexp(1.0, auto_log2))
-                ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
-                : ct;
-        rc = timed(p, s, 2, 8.0 * M * N * K * nbatch, [&]() -> int32_t {
-          st = bl.gemm(D.handle, CUBLAS_OP_T, CUBLAS_OP_N, (int)mr, (int)nr, (int)(2 * K), &one, A.op[0].dst, dt,
-                       (int)(2 * K), sa, A.op[1].dst, dt, (int)(2 * K), sb, &zero, C, dt, (int)mr, 2 * M * N, nbatch,
-                       cts, CUBLAS_GEMM_DEFAULT);
-          if (st != CUBLAS_STATUS_SUCCESS) return blas_fail("tedq_tn_contract: cublasGemmStridedBatchedEx", st);
+        TnGemmArgs G;
+        G.a = A.op[0].dst;
+        G.b = A.op[1].dst;
+        G.c = C;
+        G.mr = mr;
+        G.nr = nr;
+        G.kr = 2 * K;
+        G.sa = A.op[0].nb > 1 ? mr * 2 * K : 0;
+        G.sb = A.op[1].nb > 1 ? nr * 2 * K : 0;
+        G.sc = 2 * M * N;
+        G.nbatch = nbatch;
+        G.err = D.err;
+        // GEMM arithmetic: FP64 FMA (complex128); FP32 FMA; tensor cores with
+        // one TF32 product (TF32) or the 3xTF32 split (TC32, AUTO above the
+        // threshold) where the shape fills the tensor-core tiles
+        int path = 0;  // 0 FMA, 1 3xTF32, 2 TF32
+        if (!dbl && tn_gemm_tc_supported(G)) {
+          if (p->gemm == TEDQ_TN_GEMM_TC32) path = 1;
+          else if (p->gemm == TEDQ_TN_GEMM_TF32) path = 2;
+          else if (p->gemm == TEDQ_TN_GEMM_AUTO && 8.0 * M * N * K >= std::ldexp(1.0, auto_log2)) path = 1;
+        }
+        rc = timed(p, s, path ? 4 : 2, 8.0 * M * N * K * nbatch, [&]() -> int32_t {
+          TEDQ_CUDA("tedq_tn_contract: GEMM kernel",
+                    path ? tn_gemm_tc(G, path == 1, s) : tn_gemm_simt<real>(G, s));
           return TEDQ_OK;
         });
         if (rc != TEDQ_OK) return rc;
@@ -571,7 +495,7 @@ int32_t enqueue(tedq_tn_plan* p, TnDevice& D, const real* params, int64_t batch,
       int32_t rc = timed(p, s, 3, 0.0, [&]() -> int32_t {
         TEDQ_CUDA("tedq_tn_contract: root kernel",
                   tn_root<real>(root, R.batched ? 2 : 0, batch, acc, out, n_meas, m, sl == 0, sl == n_slices - 1,
-                                params, p->n_params, s));
+                                params, p->n_params, D.err, s));
         return TEDQ_OK;
       });
       if (rc != TEDQ_OK) return rc;
@@ -626,14 +550,14 @@ void release_devices(tedq_tn_plan* p) {
   cudaGetDevice(&cur);
   for (int d = 0; d < 64; ++d) {
     TnDevice& D = p->dev[d];
-    if (!D.handle && !D.consts && !D.desc && !D.exec && !D.capture && !D.items) continue;
+    if (!D.err && !D.consts && !D.desc && !D.exec && !D.capture && !D.items) continue;
     cudaSetDevice(d);
     if (D.exec) cudaGraphExecDestroy(D.exec);
     if (D.capture) cudaStreamDestroy(D.capture);
     if (D.consts) cudaFree(D.consts);
     if (D.desc) cudaFree(D.desc);
     if (D.items) cudaFree(D.items);
-    if (D.handle) blas().destroy(D.handle);
+    if (D.err) cudaFree(D.err);
     D = TnDevice();
   }
   cudaSetDevice(cur);
@@ -808,6 +732,43 @@ int32_t tedq_tn_profile_enable(tedq_tn_plan_t* plan, int32_t on) {
   return TEDQ_OK;
 }
 
+int32_t tedq_tn_gemm(int32_t precision, int32_t gemm, const void* a, const void* b, void* c, int64_t mr, int64_t nr,
+                     int64_t kr, int64_t sa, int64_t sb, int64_t sc, int64_t nbatch, int32_t* err_word, void* stream) {
+  if (!a || !b || !c) return fail(TEDQ_ERR_ARG, "tedq_tn_gemm: null operand");
+  if (mr < 1 || nr < 1 || kr < 1 || nbatch < 1 || nbatch > 65535 || sa < 0 || sb < 0 || sc < 0)
+    return fail(TEDQ_ERR_ARG, "tedq_tn_gemm: sizes out of range");
+  if (precision != TEDQ_PREC_C64 && precision != TEDQ_PREC_C128)
+    return fail(TEDQ_ERR_ARG, "tedq_tn_gemm: unknown precision");
+  if (gemm < TEDQ_TN_GEMM_FP32 || gemm > TEDQ_TN_GEMM_AUTO) return fail(TEDQ_ERR_ARG, "tedq_tn_gemm: unknown mode");
+  TnGemmArgs G;
+  G.a = a;
+  G.b = b;
+  G.c = c;
+  G.mr = mr;
+  G.nr = nr;
+  G.kr = kr;
+  G.sa = sa;
+  G.sb = sb;
+  G.sc = sc;
+  G.nbatch = nbatch;
+  G.err = err_word;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (precision == TEDQ_PREC_C128) {
+    e = tn_gemm_simt<double>(G, s);
+  } else if (gemm == TEDQ_TN_GEMM_FP32) {
+    e = tn_gemm_simt<float>(G, s);
+  } else {
+    const bool tc = err_word && tn_gemm_tc_supported(G);
+    if (!tc && gemm != TEDQ_TN_GEMM_AUTO)
+      return fail(TEDQ_ERR_UNSUPPORTED, "tedq_tn_gemm: shape, alignment or missing error word rules out the "
+                                        "tensor-core kernel");
+    e = tc ? tn_gemm_tc(G, gemm != TEDQ_TN_GEMM_TF32, s) : tn_gemm_simt<float>(G, s);
+  }
+  if (e != cudaSuccess) return cuda_fail("tedq_tn_gemm", e);
+  return TEDQ_OK;
+}
+
 int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out) {
   if (!plan || !out) return fail(TEDQ_ERR_ARG, "tedq_tn_profile_read: null argument");
   std::vector<tedq_tn_plan::Ev> evs;
@@ -826,10 +787,24 @@ int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out) {
       case 0: out->leaf_launches++; out->leaf_ms += ms; break;
       case 1: out->gather_launches++; out->gather_ms += ms; out->gather_bytes += e.work; break;
       case 2: out->gemm_launches++; out->gemm_ms += ms; out->gemm_flops += e.work; break;
+      case 4:
+        out->gemm_launches++; out->gemm_ms += ms; out->gemm_flops += e.work;
+        out->tc_launches++; out->tc_ms += ms; out->tc_flops += e.work;
+        break;
       default: out->root_launches++; out->root_ms += ms; break;
     }
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
+  }
+  // error word of the tensor-core GEMMs on the current device
+  int dev = 0;
+  if (rc == TEDQ_OK && cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && plan->dev[dev].err) {
+    int word = 0;
+    cudaError_t e = cudaMemcpy(&word, plan->dev[dev].err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail("tedq_tn_profile_read", e);
+    out->gemm_error = word;
+    if (word) rc = fail(TEDQ_ERR_TIMEOUT, "tedq_tn_profile_read: a tensor-core GEMM gave up a bounded wait (code " +
+                                             std::to_string(word) + "); its results are NaN");
   }
   return rc;
 }

@@ -1,0 +1,523 @@
+// tn_gemm.cu -- batched real GEMMs of the tensor-network mode (the pairwise
+// contractions of the 4M real embedding), hand-written for sm_103a.
+//
+//   C[b](i, j) = sum_k A[b](i, k) * B[b](j, k),  C column-major (i fastest,
+//   leading dimension mr), A [mr][kr] and B [nr][kr] K-contiguous (the rows
+//   the operand gathers write).
+//
+// FP32-accurate tensor-core path (complex64 plans): tcgen05.mma kind::tf32
+// with the 3xTF32 split.  Each operand x is split in shared memory into
+// hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the accumulator in
+// tensor memory receives hi*hi + hi*lo + lo*hi (the dropped lo*lo term and
+// the rounding of lo are below 2^-21 relative).  One CTA computes a 128-row
+// tile of the larger side (the "P" operand) against a BN-column tile of the
+// other ("Q"), BN in {16, 32, 64}; six warps:
+//   warp 0     TMA producer: 3-D tensor maps [batch][rows][k], 128-byte
+//              swizzle, boxes of 32 K-elements (one swizzle row);
+//   warp 1     allocates the tensor-memory accumulator and issues the MMAs
+//              (one thread), commits each stage back to the producer;
+//   warps 2-5  split each landed stage into hi/lo tiles (element-wise on the
+//              swizzled image, so no address arithmetic), then read the
+//              accumulator with tcgen05.ld (one 32-lane quadrant per warp)
+//              and store C.
+// Every mbarrier wait is bounded; a wait that gives up sets the device error
+// word (read by the root kernel, which then returns NaN) and the CTA drains
+// and frees its tensor memory before returning.
+//
+// A shared-memory-tiled SIMT kernel (FP32 or FP64 FMA) serves the complex128
+// plans, the FP32 mode and the shapes too small for a 128-row tile.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tn_gemm.cuh"
+
+namespace tedq {
+
+namespace {
+
+// ------------------------------------------------------------------ PTX helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: about half a second of polling, then the error word is set
+// and false returned.  Once any CTA has set the word, the others give up
+// their waits at the next check instead of polling to their own limit.
+constexpr uint32_t kWaitTries = 1u << 21;
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code, bool bail = true) {
+  for (uint32_t t = 0; t < kWaitTries; ++t) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (t > 64) {
+      __nanosleep(t < 4096 ? 32 : 256);
+      if (bail && (t & 1023) == 0 && *(volatile int*)err != 0) return false;
+    }
+  }
+  atomicExch(err, code);
+  return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand in the canonical 128-byte
+// swizzled layout (8-row atoms of 128 bytes, atoms 1024 bytes apart).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);        // start address
+  d |= (uint64_t)(1) << 16;                        // leading byte offset (unused for K-major swizzled)
+  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // stride byte offset: 8 rows x 128 bytes
+  d |= (uint64_t)1 << 46;                          // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                          // layout: 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_tf32(int n) {
+  return (1u << 4)                       // D format: F32
+         | (2u << 7)                     // A format: TF32
+         | (2u << 10)                    // B format: TF32
+         | ((uint32_t)(n >> 3) << 17)    // N / 8
+         | ((uint32_t)(128 >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 8 consecutive accumulator columns of this thread's lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// ------------------------------------------------------------------ tensor-core kernel
+
+constexpr int kTcThreads = 192;  // 6 warps
+constexpr int kKBlock = 32;      // K elements per stage (one 128-byte swizzle row)
+constexpr int kStages = 2;
+
+template <int BN>
+struct TcSmem {
+  static constexpr int kA = 128 * kKBlock * 4;  // bytes of one P tile
+  static constexpr int kB = BN * kKBlock * 4;   // bytes of one Q tile
+  static constexpr int kStage = 2 * (kA + kB);  // hi and lo of both
+  static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 256 /* barriers */;
+};
+
+// C element of tile row p (P side) and column q (Q side)
+struct TcOut {
+  float* c;
+  int64_t sc;     // reals between batch entries of C
+  int64_t ldc;    // mr
+  int32_t swap;   // 0: p = i (rows of C), q = j; 1: p = j, q = i
+  int32_t p_ext, q_ext;
+};
+
+template <int BN, bool SPLIT>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tn_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_p, const __grid_constant__ CUtensorMap map_q,
+                      const TcOut out, int kblocks, int p_batched, int q_batched, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  using S = TcSmem<BN>;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::kStage);  // TMA landed
+  uint64_t* split = full + kStages;                                          // hi/lo written
+  uint64_t* empty = split + kStages;                                         // MMAs of the stage done
+  uint64_t* done = empty + kStages;                                          // accumulator complete
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile_p = blockIdx.x * 128, tile_q = blockIdx.y * BN, batch = blockIdx.z;
+  constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&split[s], SPLIT ? 4 : 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    fence_proxy_async();
+    prefetch_map(&map_p);
+    prefetch_map(&map_q);
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, kCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+
+  int issued = 0;  // k-blocks whose loads the producer issued
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < kblocks && ok; ++kb) {
+        const int s = kb % kStages;
+        if (kb >= kStages) ok = mbar_wait(&empty[s], ((kb / kStages) - 1) & 1, err, 1);
+        if (!ok) break;
+        unsigned char* st = smem + s * S::kStage;
+        mbar_expect_tx(&full[s], S::kA + S::kB);
+        tma_load_3d(st, &map_p, &full[s], kb * kKBlock, tile_p, p_batched ? batch : 0);
+        tma_load_3d(st + S::kA, &map_q, &full[s], kb * kKBlock, tile_q, q_batched ? batch : 0);
+        issued = kb + 1;
+      }
+      // every issued copy has landed before the CTA may exit (immediate on the
+      // normal path, where the consumers waited for them already)
+      for (int kb = issued > kStages ? issued - kStages : 0; kb < issued; ++kb)
+        mbar_wait(&full[kb % kStages], (kb / kStages) & 1, err, 6, false);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(BN);
+      for (int kb = 0; kb < kblocks && ok; ++kb) {
+        const int s = kb % kStages;
+        const uint32_t par = (kb / kStages) & 1;
+        ok = SPLIT ? mbar_wait(&split[s], par, err, 2) : mbar_wait(&full[s], par, err, 2);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t st = smem_u32(smem + s * S::kStage);
+        const uint32_t a_hi = st, b_hi = st + S::kA, a_lo = st + S::kA + S::kB, b_lo = a_lo + S::kA;
+#pragma unroll
+        for (int k = 0; k < kKBlock / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
+          const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+          mma_tf32(tmem, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, acc);
+          if (SPLIT) {
+            mma_tf32(tmem, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, 1u);
+            mma_tf32(tmem, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+          }
+        }
+        mma_commit(&empty[s]);  // frees the stage when these MMAs have read it
+      }
+      mma_commit(done);
+    }
+  } else {
+    // warps 2-5: split the stages, then the epilogue
+    const int t = threadIdx.x - 64;  // 0..127
+    if (SPLIT) {
+      for (int kb = 0; kb < kblocks && ok; ++kb) {
+        const int s = kb % kStages;
+        ok = mbar_wait(&full[s], (kb / kStages) & 1, err, 3);
+        if (!ok) break;
+        unsigned char* st = smem + s * S::kStage;
+        float4* hi = reinterpret_cast<float4*>(st);                 // A tile then B tile
+        float4* lo = reinterpret_cast<float4*>(st + S::kA + S::kB);  // same order
+        constexpr int n4 = (S::kA + S::kB) / 16;
+        for (int i = t; i < n4; i += 128) {
+          float4 x = hi[i], h, l;
+          h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
+          h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
+          h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
+          h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+          hi[i] = h;
+          lo[i] = l;
+        }
+        fence_proxy_async();  // generic-proxy writes -> visible to the tensor cores
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&split[s]);
+      }
+    }
+    // epilogue: this warp's 32-lane quadrant of the accumulator (the
+    // tensor-memory loads are warp-collective: the decision is warp-uniform)
+    if (ok) ok = mbar_wait(done, 0, err, 4);
+    ok = __all_sync(0xffffffffu, ok);
+    if (ok) {
+      tc_fence_after();
+      const int quad = warp & 3;
+      const int p = tile_p + quad * 32 + lane;
+      float* cb = out.c + (int64_t)batch * out.sc;
+#pragma unroll
+      for (int c0 = 0; c0 < BN; c0 += 8) {
+        float v[8];
+        tmem_ld8(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
+        if (p < out.p_ext) {
+          if (!out.swap) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int q = tile_q + c0 + j;
+              if (q < out.q_ext) cb[(int64_t)q * out.ldc + p] = v[j];
+            }
+          } else {
+            const int q = tile_q + c0;
+            float* dst = cb + (int64_t)p * out.ldc + q;
+            if (q + 8 <= out.q_ext && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
+              reinterpret_cast<float4*>(dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
+              reinterpret_cast<float4*>(dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
+            } else {
+#pragma unroll
+              for (int j = 0; j < 8; ++j)
+                if (q + j < out.q_ext) dst[j] = v[j];
+            }
+          }
+        }
+      }
+    }
+  }
+  // no MMA may still write the accumulator when it is freed: the final commit
+  // (already complete on the normal path) is awaited, bounded
+  if (threadIdx.x == 64) mbar_wait(done, 0, err, 5, false);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kCols);
+  }
+}
+
+// ------------------------------------------------------------------ SIMT kernel
+
+// Tile BM x BN of C, K in chunks of 16 through shared memory; each thread
+// computes TM x TN outputs.  A [P][kr] and B [Q][kr] K-contiguous.
+template <typename real, int BM, int BN, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    tn_gemm_simt_kernel(const real* __restrict__ a, const real* __restrict__ b, real* __restrict__ c, int64_t mr,
+                        int64_t nr, int64_t kr, int64_t sa, int64_t sb, int64_t sc) {
+  constexpr int BK = 16;
+  constexpr int T = (BM / TM) * (BN / TN);
+  __shared__ real As[BK][BM + 1];
+  __shared__ real Bs[BK][BN + 1];
+  const int64_t bt = blockIdx.z;
+  const real* A = a + bt * sa;
+  const real* B = b + bt * sb;
+  real* C = c + bt * sc;
+  const int64_t i0 = (int64_t)blockIdx.x * BM, j0 = (int64_t)blockIdx.y * BN;
+  const int tid = threadIdx.x;
+  const int ti = tid % (BM / TM), tj = tid / (BM / TM);
+  real acc[TM][TN];
+#pragma unroll
+  for (int x = 0; x < TM; ++x)
+#pragma unroll
+    for (int y = 0; y < TN; ++y) acc[x][y] = 0;
+  for (int64_t k0 = 0; k0 < kr; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += T) {
+      const int r = e / BK, k = e % BK;
+      const int64_t gi = i0 + r, gk = k0 + k;
+      As[k][r] = (gi < mr && gk < kr) ? A[gi * kr + gk] : (real)0;
+    }
+    for (int e = tid; e < BN * BK; e += T) {
+      const int r = e / BK, k = e % BK;
+      const int64_t gj = j0 + r, gk = k0 + k;
+      Bs[k][r] = (gj < nr && gk < kr) ? B[gj * kr + gk] : (real)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      real av[TM], bv[TN];
+#pragma unroll
+      for (int x = 0; x < TM; ++x) av[x] = As[k][ti + x * (BM / TM)];
+#pragma unroll
+      for (int y = 0; y < TN; ++y) bv[y] = Bs[k][tj + y * (BN / TN)];
+#pragma unroll
+      for (int x = 0; x < TM; ++x)
+#pragma unroll
+        for (int y = 0; y < TN; ++y) acc[x][y] = fma(av[x], bv[y], acc[x][y]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int y = 0; y < TN; ++y) {
+    const int64_t gj = j0 + tj + y * (BN / TN);
+#pragma unroll
+    for (int x = 0; x < TM; ++x) {
+      const int64_t gi = i0 + ti + x * (BM / TM);
+      if (gi < mr && gj < nr) C[gj * mr + gi] = acc[x][y];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static EncodeTiled fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// [batch][rows][kr] FP32, box [1][box_rows][32], 128-byte swizzle; rows and
+// K beyond the extents read as zero
+bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t kr, int64_t batch, int64_t bstride,
+              int box_rows) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)kr, (cuuint64_t)rows, (cuuint64_t)(bstride ? batch : 1)};
+  const cuuint64_t strides[2] = {(cuuint64_t)kr * 4, (cuuint64_t)(bstride ? bstride : rows * kr) * 4};
+  const cuuint32_t box[3] = {32, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, bool SPLIT>
+cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcOut& o, int64_t p_ext, int64_t q_ext,
+                      int kblocks, int64_t nbatch, int pb, int qb, int* err, cudaStream_t s) {
+  const int bytes = TcSmem<BN>::kBytes;
+  static bool attr[64] = {false};  // per device (setting it twice is harmless)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(tn_gemm_tc_kernel<BN, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         bytes);
+    if (e != cudaSuccess) return e;
+    attr[dev] = true;
+  }
+  dim3 grid((unsigned)((p_ext + 127) / 128), (unsigned)((q_ext + BN - 1) / BN), (unsigned)nbatch);
+  tn_gemm_tc_kernel<BN, SPLIT><<<grid, kTcThreads, bytes, s>>>(mp, mq, o, kblocks, pb, qb, err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool tn_gemm_tc_supported(const TnGemmArgs& g) {
+  // FP32 rows of kr reals: 16-byte TMA strides and bases; the P side fills a
+  // 128-row tile to at least a quarter, the Q side at least 8 columns
+  const int64_t P = g.mr >= g.nr ? g.mr : g.nr, Q = g.mr >= g.nr ? g.nr : g.mr;
+  return g.kr % 4 == 0 && g.kr >= 8 && P >= 32 && Q >= 8 && g.nbatch <= 65535 &&
+         (reinterpret_cast<uintptr_t>(g.a) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.b) & 15) == 0 &&
+         (g.sa * 4) % 16 == 0 && (g.sb * 4) % 16 == 0 && encode_fn() != nullptr;
+}
+
+cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
+  // the larger side fills the 128-row tiles
+  const bool swap = g.nr > g.mr;
+  const float* P = static_cast<const float*>(swap ? g.b : g.a);
+  const float* Q = static_cast<const float*>(swap ? g.a : g.b);
+  const int64_t pe = swap ? g.nr : g.mr, qe = swap ? g.mr : g.nr;
+  const int64_t sp = swap ? g.sb : g.sa, sq = swap ? g.sa : g.sb;
+  const int bn = qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
+  CUtensorMap mp, mq;
+  if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn))
+    return cudaErrorInvalidValue;
+  TcOut o;
+  o.c = static_cast<float*>(g.c);
+  o.sc = g.sc;
+  o.ldc = g.mr;
+  o.swap = swap ? 1 : 0;
+  o.p_ext = (int32_t)pe;
+  o.q_ext = (int32_t)qe;
+  const int kblocks = (int)((g.kr + kKBlock - 1) / kKBlock);
+  const int pb = sp != 0, qb = sq != 0;
+  if (split) {
+    if (bn == 64) return launch_tc<64, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+    if (bn == 32) return launch_tc<32, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+    return launch_tc<16, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+  }
+  if (bn == 64) return launch_tc<64, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+  if (bn == 32) return launch_tc<32, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+  return launch_tc<16, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+}
+
+template <typename real>
+cudaError_t tn_gemm_simt(const TnGemmArgs& g, cudaStream_t s) {
+  const real* A = static_cast<const real*>(g.a);
+  const real* B = static_cast<const real*>(g.b);
+  real* C = static_cast<real*>(g.c);
+  if (g.mr >= 64 && g.nr >= 64) {
+    dim3 grid((unsigned)((g.mr + 63) / 64), (unsigned)((g.nr + 63) / 64), (unsigned)g.nbatch);
+    tn_gemm_simt_kernel<real, 64, 64, 4, 4><<<grid, 256, 0, s>>>(A, B, C, g.mr, g.nr, g.kr, g.sa, g.sb, g.sc);
+  } else {
+    dim3 grid((unsigned)((g.mr + 15) / 16), (unsigned)((g.nr + 15) / 16), (unsigned)g.nbatch);
+    tn_gemm_simt_kernel<real, 16, 16, 1, 1><<<grid, 256, 0, s>>>(A, B, C, g.mr, g.nr, g.kr, g.sa, g.sb, g.sc);
+  }
+  return cudaGetLastError();
+}
+
+template cudaError_t tn_gemm_simt<float>(const TnGemmArgs&, cudaStream_t);
+template cudaError_t tn_gemm_simt<double>(const TnGemmArgs&, cudaStream_t);
+
+}  // namespace tedq

@@ -6,8 +6,9 @@
 //    writes the planar complex result;
 //  * large ones: one gather launch writes both operands as rows of the real
 //    embedding ([Re, Im], and [Re, -Im] / [Im, Re] for the doubled operand),
-//    then one real GEMM over the batch (cuBLAS; BF16x9 tensor-core emulation
-//    or FP32) produces [Re C, Im C] -- the 4M decomposition in one product.
+//    then one real GEMM over the batch (tn_gemm.cu: tcgen05 tensor cores with
+//    the 3xTF32 split, or FP32 / FP64 FMA) produces [Re C, Im C] -- the 4M
+//    decomposition in one product.
 // Gather traffic per operand entry (c64): 8 B read, 8 B written (16 B for the
 // doubled operand).
 #include <cuda_runtime.h>
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(256) tn_fused_level_kernel(const TnFusedItem* 
 template <typename real>
 __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, int64_t batch, double* acc,
                                real* out, int n_meas, int m, int first, int last, const real* __restrict__ prm,
-                               int n_params) {
+                               int n_params, const int* err) {
   const int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (b >= batch) return;
@@ -399,6 +400,8 @@ __global__ void tn_root_kernel(const real* __restrict__ root, int64_t bstride, i
   if (last)
     for (int j = lane; j < n_params; j += 32) finite &= isfinite(prm[b * n_params + j]);
   finite = __all_sync(0xffffffffu, finite);
+  // a contraction kernel that gave up a bounded wait leaves every result invalid
+  if (last && err && *(volatile const int*)err != 0) finite = false;
   if (lane) return;
   const real* p = root + b * bstride;
   double v = (double)p[0];
@@ -456,10 +459,11 @@ cudaError_t tn_fused_level(const TnFusedItem* items, int n_items, int blocks, ch
 
 template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
-                    int m, int first, int last, const real* params, int n_params, cudaStream_t stream) {
+                    int m, int first, int last, const real* params, int n_params, const int* err,
+                    cudaStream_t stream) {
   const unsigned blocks = (unsigned)((batch * 32 + 255) / 256);
   return launch_kernel(tn_root_kernel<real>, dim3(blocks), dim3(256), 0, stream, root, root_bstride, batch, acc, out,
-                       n_meas, m, first, last, params, n_params);
+                       n_meas, m, first, last, params, n_params, err);
 }
 
 template cudaError_t tn_build_leaves<float>(const TnLeafDesc*, int, const float*, int, int64_t, float*, cudaStream_t);
@@ -473,8 +477,8 @@ template cudaError_t tn_fused_level<float>(const TnFusedItem*, int, int, char*, 
 template cudaError_t tn_fused_level<double>(const TnFusedItem*, int, int, char*, const void*, int64_t,
                                             cudaStream_t);
 template cudaError_t tn_root<float>(const float*, int64_t, int64_t, double*, float*, int, int, int, int,
-                                    const float*, int, cudaStream_t);
+                                    const float*, int, const int*, cudaStream_t);
 template cudaError_t tn_root<double>(const double*, int64_t, int64_t, double*, double*, int, int, int, int,
-                                     const double*, int, cudaStream_t);
+                                     const double*, int, const int*, cudaStream_t);
 
 }  // namespace tedq

@@ -1,7 +1,7 @@
 // tn_kernels.cuh -- device side of the tensor-network mode: batched gate
 // tensors from the parameters, operand gathers (bit permutations into planar
 // real GEMM operands) and the FP64 root accumulation.  The GEMMs themselves
-// are cuBLAS strided-batched calls issued by tn_capi.cpp.
+// are in tn_gemm.cu.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -118,9 +118,10 @@ template <typename real>
 cudaError_t tn_gather(const TnGatherArgs& args, cudaStream_t stream);
 // acc[b * n_meas + m] (+)= Re(root) for every circuit b (first: assign);
 // last: out[b * n_meas + m] = acc (NaN for a circuit with a non-finite
-// parameter).
+// parameter, and for every circuit when the device error word `err` is set).
 template <typename real>
 cudaError_t tn_root(const real* root, int64_t root_bstride, int64_t batch, double* acc, real* out, int n_meas,
-                    int m, int first, int last, const real* params, int n_params, cudaStream_t stream);
+                    int m, int first, int last, const real* params, int n_params, const int* err,
+                    cudaStream_t stream);
 
 }  // namespace tedq

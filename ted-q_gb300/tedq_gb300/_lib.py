@@ -95,10 +95,11 @@ class TnProfile(ctypes.Structure):
     _fields_ = [("leaf_launches", c_int64), ("leaf_ms", c_double), ("gather_launches", c_int64),
                 ("gather_ms", c_double), ("gather_bytes", c_double), ("gemm_launches", c_int64),
                 ("gemm_ms", c_double), ("gemm_flops", c_double), ("root_launches", c_int64), ("root_ms", c_double),
-                ("reserved", c_int64 * 4)]
+                ("tc_launches", c_int64), ("tc_ms", c_double), ("tc_flops", c_double), ("gemm_error", c_int32),
+                ("pad", c_int32)]
 
 
-TN_GEMM = {"fp32": 0, "bf16x9": 1, "tf32": 2, "auto": 3}
+TN_GEMM = {"fp32": 0, "tc32": 1, "tf32": 2, "auto": 3}
 
 # every symbol the header declares, with (restype, argtypes)
 SIGNATURES = {
@@ -134,6 +135,8 @@ SIGNATURES = {
     "tedq_tn_contract": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tedq_tn_profile_enable": (c_int32, [c_void_p, c_int32]),
     "tedq_tn_profile_read": (c_int32, [c_void_p, POINTER(TnProfile)]),
+    "tedq_tn_gemm": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_int64, c_int64, c_int64,
+                               c_int64, c_int64, c_int64, c_void_p, c_void_p]),
 }
 
 _lib = None
