@@ -9,7 +9,11 @@
 // with the 3xTF32 split.  Each operand x is split in shared memory into
 // hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the accumulator in
 // tensor memory receives hi*hi + hi*lo + lo*hi (the dropped lo*lo term and
-// the rounding of lo are below 2^-21 relative).  One CTA computes a 128-row
+// the rounding of lo are below 2^-21 relative).  The tensor cores' own
+// accumulation truncates: each 32-wide K-block is accumulated in a fresh
+// tensor-memory buffer (two, alternating) and the blocks are summed in FP32
+// registers with round-to-nearest, which keeps the result at FP32 accuracy
+// for long K.  One CTA computes a 128-row
 // tile of the larger side (the "P" operand) against a BN-column tile of the
 // other ("Q"), BN in {16, 32, 64}; six warps:
 //   warp 0     TMA producer: 3-D tensor maps [batch][rows][k], 128-byte
@@ -17,9 +21,9 @@
 //   warp 1     allocates the tensor-memory accumulator and issues the MMAs
 //              (one thread), commits each stage back to the producer;
 //   warps 2-5  split each landed stage into hi/lo tiles (element-wise on the
-//              swizzled image, so no address arithmetic), then read the
-//              accumulator with tcgen05.ld (one 32-lane quadrant per warp)
-//              and store C.
+//              swizzled image, so no address arithmetic), add each K-block's
+//              partial sum from tensor memory (tcgen05.ld, one 32-lane
+//              quadrant per warp) into registers, and store C.
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by the root kernel, which then returns NaN) and the CTA drains
 // and frees its tensor memory before returning.
@@ -186,6 +190,7 @@ struct TcSmem {
   static constexpr int kB = BN * kKBlock * 4;   // bytes of one Q tile
   static constexpr int kStage = 2 * (kA + kB);  // hi and lo of both
   static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 256 /* barriers */;
+  static_assert(4 * kStages * 8 + 5 * 8 + 4 <= 256, "barrier region");
 };
 
 // C element of tile row p (P side) and column q (Q side)
@@ -207,17 +212,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::kStage);  // TMA landed
   uint64_t* split = full + kStages;                                          // hi/lo written
   uint64_t* empty = split + kStages;                                         // MMAs of the stage done
-  uint64_t* done = empty + kStages;                                          // accumulator complete
+  uint64_t* accf = empty + kStages;   // [2] k-block partial complete in accumulator buffer b
+  uint64_t* acce = accf + 2;          // [2] accumulator buffer b read back
+  uint64_t* done = acce + 2;          // every MMA complete
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tile_p = blockIdx.x * 128, tile_q = blockIdx.y * BN, batch = blockIdx.z;
-  constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+  // two accumulator buffers of BN columns: the MMAs of a K-block write one
+  // while the epilogue warps add the other into FP32 registers
+  constexpr uint32_t kCols = 2 * BN < 32 ? 32 : 2 * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&split[s], SPLIT ? 4 : 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
     }
     mbar_init(done, 1);
     fence_proxy_async();
@@ -253,82 +266,103 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BN);
       for (int kb = 0; kb < kblocks && ok; ++kb) {
-        const int s = kb % kStages;
+        const int s = kb % kStages, buf = kb & 1;
         const uint32_t par = (kb / kStages) & 1;
+        if (kb >= 2) ok = mbar_wait(&acce[buf], ((kb >> 1) - 1) & 1, err, 7);  // buffer read back
+        if (!ok) break;
         ok = SPLIT ? mbar_wait(&split[s], par, err, 2) : mbar_wait(&full[s], par, err, 2);
         if (!ok) break;
         tc_fence_after();
         const uint32_t st = smem_u32(smem + s * S::kStage);
         const uint32_t a_hi = st, b_hi = st + S::kA, a_lo = st + S::kA + S::kB, b_lo = a_lo + S::kA;
+        const uint32_t d = tmem + (uint32_t)(buf * BN);
 #pragma unroll
         for (int k = 0; k < kKBlock / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
-          const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-          mma_tf32(tmem, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, acc);
+          mma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, k > 0 ? 1u : 0u);
           if (SPLIT) {
-            mma_tf32(tmem, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, 1u);
-            mma_tf32(tmem, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+            mma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, 1u);
+            mma_tf32(d, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
           }
         }
-        mma_commit(&empty[s]);  // frees the stage when these MMAs have read it
+        mma_commit(&empty[s]);    // frees the stage when these MMAs have read it
+        mma_commit(&accf[buf]);   // the K-block's partial sum is ready
       }
       mma_commit(done);
     }
   } else {
-    // warps 2-5: split the stages, then the epilogue
+    // warps 2-5: split each landed stage into hi / lo, and add each K-block's
+    // partial sum (tensor memory, this warp's 32-lane quadrant) into FP32
+    // registers with round-to-nearest additions
     const int t = threadIdx.x - 64;  // 0..127
-    if (SPLIT) {
-      for (int kb = 0; kb < kblocks && ok; ++kb) {
-        const int s = kb % kStages;
-        ok = mbar_wait(&full[s], (kb / kStages) & 1, err, 3);
-        if (!ok) break;
-        unsigned char* st = smem + s * S::kStage;
-        float4* hi = reinterpret_cast<float4*>(st);                 // A tile then B tile
-        float4* lo = reinterpret_cast<float4*>(st + S::kA + S::kB);  // same order
-        constexpr int n4 = (S::kA + S::kB) / 16;
-        for (int i = t; i < n4; i += 128) {
-          float4 x = hi[i], h, l;
-          h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
-          h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
-          h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
-          h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
-          hi[i] = h;
-          lo[i] = l;
-        }
-        fence_proxy_async();  // generic-proxy writes -> visible to the tensor cores
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&split[s]);
+    const int quad = warp & 3;
+    float acc[BN];
+#pragma unroll
+    for (int j = 0; j < BN; ++j) acc[j] = 0.f;
+    auto split_stage = [&](int kb) {
+      const int s = kb % kStages;
+      ok = mbar_wait(&full[s], (kb / kStages) & 1, err, 3);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) return;
+      unsigned char* st = smem + s * S::kStage;
+      float4* hi = reinterpret_cast<float4*>(st);                  // P tile then Q tile
+      float4* lo = reinterpret_cast<float4*>(st + S::kA + S::kB);  // same order
+      constexpr int n4 = (S::kA + S::kB) / 16;
+      for (int i = t; i < n4; i += 128) {
+        float4 x = hi[i], h, l;
+        h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
+        h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
+        h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
+        h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+        hi[i] = h;
+        lo[i] = l;
       }
-    }
-    // epilogue: this warp's 32-lane quadrant of the accumulator (the
-    // tensor-memory loads are warp-collective: the decision is warp-uniform)
-    if (ok) ok = mbar_wait(done, 0, err, 4);
-    ok = __all_sync(0xffffffffu, ok);
-    if (ok) {
+      fence_proxy_async();  // generic-proxy writes -> visible to the tensor cores
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&split[s]);
+    };
+    auto flush = [&](int kb) {
+      const int buf = kb & 1;
+      ok = mbar_wait(&accf[buf], (kb >> 1) & 1, err, 4);
+      ok = __all_sync(0xffffffffu, ok);  // tensor-memory loads are warp-collective
+      if (!ok) return;
       tc_fence_after();
-      const int quad = warp & 3;
-      const int p = tile_p + quad * 32 + lane;
-      float* cb = out.c + (int64_t)batch * out.sc;
+      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
 #pragma unroll
       for (int c0 = 0; c0 < BN; c0 += 8) {
         float v[8];
-        tmem_ld8(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
-        if (p < out.p_ext) {
-          if (!out.swap) {
+        tmem_ld8(base + (uint32_t)c0, v);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int q = tile_q + c0 + j;
-              if (q < out.q_ext) cb[(int64_t)q * out.ldc + p] = v[j];
-            }
-          } else {
-            const int q = tile_q + c0;
-            float* dst = cb + (int64_t)p * out.ldc + q;
-            if (q + 8 <= out.q_ext && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0)) {
-              reinterpret_cast<float4*>(dst)[0] = make_float4(v[0], v[1], v[2], v[3]);
-              reinterpret_cast<float4*>(dst)[1] = make_float4(v[4], v[5], v[6], v[7]);
+        for (int j = 0; j < 8; ++j) acc[c0 + j] += v[j];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
+    };
+    for (int kb = 0; kb <= kblocks && ok; ++kb) {
+      if (SPLIT && kb < kblocks) split_stage(kb);
+      if (ok && kb >= 1) flush(kb - 1);
+    }
+    if (ok) {
+      const int p = tile_p + quad * 32 + lane;
+      float* cb = out.c + (int64_t)batch * out.sc;
+      if (p < out.p_ext) {
+        if (!out.swap) {
+#pragma unroll
+          for (int j = 0; j < BN; ++j) {
+            const int q = tile_q + j;
+            if (q < out.q_ext) cb[(int64_t)q * out.ldc + p] = acc[j];
+          }
+        } else {
+          float* dst = cb + (int64_t)p * out.ldc + tile_q;
+          const bool vec = tile_q + BN <= out.q_ext && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
+#pragma unroll
+          for (int j = 0; j < BN; j += 4) {
+            if (vec) {
+              reinterpret_cast<float4*>(dst + j)[0] = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
             } else {
 #pragma unroll
-              for (int j = 0; j < 8; ++j)
-                if (q + j < out.q_ext) dst[j] = v[j];
+              for (int x = 0; x < 4; ++x)
+                if (tile_q + j + x < out.q_ext) dst[j + x] = acc[j + x];
             }
           }
         }
