@@ -15,15 +15,17 @@
 // registers with round-to-nearest, which keeps the result at FP32 accuracy
 // for long K.  One CTA computes a 128-row
 // tile of the larger side (the "P" operand) against a BN-column tile of the
-// other ("Q"), BN in {16, 32, 64}; six warps:
+// other ("Q"), BN in {16, 32, 64, 128}; persistent CTAs (one per SM) walk
+// their tiles with the pipeline running on across tile boundaries; ten warps:
 //   warp 0     TMA producer: 3-D tensor maps [batch][rows][k], 128-byte
 //              swizzle, boxes of 32 K-elements (one swizzle row);
 //   warp 1     allocates the tensor-memory accumulator and issues the MMAs
 //              (one thread), commits each stage back to the producer;
-//   warps 2-5  split each landed stage into hi/lo tiles (element-wise on the
+//   warps 2-9  split each landed stage into hi/lo tiles (element-wise on the
 //              swizzled image, so no address arithmetic), add each K-block's
-//              partial sum from tensor memory (tcgen05.ld, one 32-lane
-//              quadrant per warp) into registers, and store C.
+//              partial sum from tensor memory (tcgen05.ld; two warps per
+//              32-lane quadrant, half of the columns each) into registers,
+//              and store C after a tile's last K-block.
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by the root kernel, which then returns NaN) and the CTA drains
 // and frees its tensor memory before returning.
@@ -180,57 +182,77 @@ __device__ __forceinline__ float tf32_rna(float x) {
 
 // ------------------------------------------------------------------ tensor-core kernel
 
-constexpr int kTcThreads = 192;  // 6 warps
+constexpr int kTcThreads = 320;  // 10 warps
 constexpr int kKBlock = 32;      // K elements per stage (one 128-byte swizzle row)
-constexpr int kStages = 2;
+constexpr int kEpiWarps = 8;     // split + epilogue warps (two per tensor-memory lane quadrant)
 
 template <int BN>
 struct TcSmem {
   static constexpr int kA = 128 * kKBlock * 4;  // bytes of one P tile
   static constexpr int kB = BN * kKBlock * 4;   // bytes of one Q tile
   static constexpr int kStage = 2 * (kA + kB);  // hi and lo of both
-  static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 256 /* barriers */;
-  static_assert(4 * kStages * 8 + 5 * 8 + 4 <= 256, "barrier region");
+  // as many stages as fit next to the barriers in 200 KB
+  static constexpr int kStages = (200 * 1024) / kStage > 6 ? 6 : (200 * 1024) / kStage;
+  static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 512 /* barriers */;
+  static_assert(kStages >= 2, "pipeline depth");
+  static_assert((3 * kStages + 5) * 8 + 4 <= 512, "barrier region");
 };
 
-// C element of tile row p (P side) and column q (Q side)
-struct TcOut {
+// Work of one launch: tiles of 128 P-rows x BN Q-columns of every batch entry,
+// tile t = (batch, q tile, p tile) with the p tile fastest.
+struct TcWork {
   float* c;
   int64_t sc;     // reals between batch entries of C
   int64_t ldc;    // mr
   int32_t swap;   // 0: p = i (rows of C), q = j; 1: p = j, q = i
   int32_t p_ext, q_ext;
+  int32_t tiles_p, tiles_q;
+  int32_t kblocks;
+  int32_t p_batched, q_batched;
+  int64_t tiles;  // tiles_p * tiles_q * batch
 };
 
+// Persistent: CTA b processes tiles b, b + grid, ...; its producer, MMA
+// issuer and epilogue warps walk the same sequence of (tile, K-block) steps,
+// so the pipeline runs on across tile boundaries.
 template <int BN, bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tn_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_p, const __grid_constant__ CUtensorMap map_q,
-                      const TcOut out, int kblocks, int p_batched, int q_batched, int* err) {
+                      const TcWork w, int* err) {
+  using S = TcSmem<BN>;
+  constexpr int kStages = S::kStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  using S = TcSmem<BN>;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::kStage);  // TMA landed
   uint64_t* split = full + kStages;                                          // hi/lo written
   uint64_t* empty = split + kStages;                                         // MMAs of the stage done
-  uint64_t* accf = empty + kStages;   // [2] k-block partial complete in accumulator buffer b
+  uint64_t* accf = empty + kStages;   // [2] K-block partial complete in accumulator buffer b
   uint64_t* acce = accf + 2;          // [2] accumulator buffer b read back
   uint64_t* done = acce + 2;          // every MMA complete
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tile_p = blockIdx.x * 128, tile_q = blockIdx.y * BN, batch = blockIdx.z;
   // two accumulator buffers of BN columns: the MMAs of a K-block write one
   // while the epilogue warps add the other into FP32 registers
   constexpr uint32_t kCols = 2 * BN < 32 ? 32 : 2 * BN;
+  const int64_t my_tiles = w.tiles > blockIdx.x ? (w.tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t steps = my_tiles * w.kblocks;
+  auto tile_of = [&](int64_t i, int& tp, int& tq, int& b) {
+    const int64_t t = blockIdx.x + i * gridDim.x;
+    tp = (int)(t % w.tiles_p);
+    const int64_t r = t / w.tiles_p;
+    tq = (int)(r % w.tiles_q);
+    b = (int)(r / w.tiles_q);
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&split[s], SPLIT ? 4 : 1);
+      mbar_init(&split[s], SPLIT ? kEpiWarps : 1);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
+      mbar_init(&acce[b], kEpiWarps);
     }
     mbar_init(done, 1);
     fence_proxy_async();
@@ -244,31 +266,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
 
-  int issued = 0;  // k-blocks whose loads the producer issued
   if (warp == 0) {
     if (lane == 0) {
-      for (int kb = 0; kb < kblocks && ok; ++kb) {
-        const int s = kb % kStages;
-        if (kb >= kStages) ok = mbar_wait(&empty[s], ((kb / kStages) - 1) & 1, err, 1);
+      int64_t issued = 0;  // steps whose loads were issued
+      for (int64_t g = 0; g < steps && ok; ++g) {
+        const int s = (int)(g % kStages);
+        if (g >= kStages) ok = mbar_wait(&empty[s], (uint32_t)((g / kStages) - 1) & 1, err, 1);
         if (!ok) break;
+        int tp, tq, b;
+        tile_of(g / w.kblocks, tp, tq, b);
+        const int kb = (int)(g % w.kblocks);
         unsigned char* st = smem + s * S::kStage;
         mbar_expect_tx(&full[s], S::kA + S::kB);
-        tma_load_3d(st, &map_p, &full[s], kb * kKBlock, tile_p, p_batched ? batch : 0);
-        tma_load_3d(st + S::kA, &map_q, &full[s], kb * kKBlock, tile_q, q_batched ? batch : 0);
-        issued = kb + 1;
+        tma_load_3d(st, &map_p, &full[s], kb * kKBlock, tp * 128, w.p_batched ? b : 0);
+        tma_load_3d(st + S::kA, &map_q, &full[s], kb * kKBlock, tq * BN, w.q_batched ? b : 0);
+        issued = g + 1;
       }
       // every issued copy has landed before the CTA may exit (immediate on the
       // normal path, where the consumers waited for them already)
-      for (int kb = issued > kStages ? issued - kStages : 0; kb < issued; ++kb)
-        mbar_wait(&full[kb % kStages], (kb / kStages) & 1, err, 6, false);
+      for (int64_t g = issued > kStages ? issued - kStages : 0; g < issued; ++g)
+        mbar_wait(&full[g % kStages], (uint32_t)(g / kStages) & 1, err, 6, false);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BN);
-      for (int kb = 0; kb < kblocks && ok; ++kb) {
-        const int s = kb % kStages, buf = kb & 1;
-        const uint32_t par = (kb / kStages) & 1;
-        if (kb >= 2) ok = mbar_wait(&acce[buf], ((kb >> 1) - 1) & 1, err, 7);  // buffer read back
+      for (int64_t g = 0; g < steps && ok; ++g) {
+        const int s = (int)(g % kStages), buf = (int)(g & 1);
+        const uint32_t par = (uint32_t)(g / kStages) & 1;
+        if (g >= 2) ok = mbar_wait(&acce[buf], (uint32_t)((g >> 1) - 1) & 1, err, 7);  // buffer read back
         if (!ok) break;
         ok = SPLIT ? mbar_wait(&split[s], par, err, 2) : mbar_wait(&full[s], par, err, 2);
         if (!ok) break;
@@ -290,24 +315,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mma_commit(done);
     }
   } else {
-    // warps 2-5: split each landed stage into hi / lo, and add each K-block's
-    // partial sum (tensor memory, this warp's 32-lane quadrant) into FP32
-    // registers with round-to-nearest additions
-    const int t = threadIdx.x - 64;  // 0..127
-    const int quad = warp & 3;
-    float acc[BN];
+    // warps 2-9: split each landed stage into hi / lo, and add each K-block's
+    // partial sum (tensor memory: this warp's 32-lane quadrant, half of the
+    // columns) into FP32 registers with round-to-nearest additions; store a
+    // tile after its last K-block
+    constexpr int HALF = BN / 2;
+    const int t = threadIdx.x - 64;  // 0..255
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    float acc[HALF];
 #pragma unroll
-    for (int j = 0; j < BN; ++j) acc[j] = 0.f;
-    auto split_stage = [&](int kb) {
-      const int s = kb % kStages;
-      ok = mbar_wait(&full[s], (kb / kStages) & 1, err, 3);
+    for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+    auto split_stage = [&](int64_t g) {
+      const int s = (int)(g % kStages);
+      ok = mbar_wait(&full[s], (uint32_t)(g / kStages) & 1, err, 3);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) return;
       unsigned char* st = smem + s * S::kStage;
       float4* hi = reinterpret_cast<float4*>(st);                  // P tile then Q tile
       float4* lo = reinterpret_cast<float4*>(st + S::kA + S::kB);  // same order
       constexpr int n4 = (S::kA + S::kB) / 16;
-      for (int i = t; i < n4; i += 128) {
+#pragma unroll 4
+      for (int i = t; i < n4; i += 32 * kEpiWarps) {
         float4 x = hi[i], h, l;
         h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
         h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
@@ -320,15 +348,44 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&split[s]);
     };
-    auto flush = [&](int kb) {
-      const int buf = kb & 1;
-      ok = mbar_wait(&accf[buf], (kb >> 1) & 1, err, 4);
+    auto store_tile = [&](int64_t i) {
+      int tp, tq, b;
+      tile_of(i, tp, tq, b);
+      const int p = tp * 128 + quad * 32 + lane;
+      const int q0 = tq * BN + half * HALF;
+      float* cb = w.c + (int64_t)b * w.sc;
+      if (p < w.p_ext) {
+        if (!w.swap) {
+#pragma unroll
+          for (int j = 0; j < HALF; ++j)
+            if (q0 + j < w.q_ext) cb[(int64_t)(q0 + j) * w.ldc + p] = acc[j];
+        } else {
+          float* dst = cb + (int64_t)p * w.ldc + q0;
+          const bool vec = q0 + HALF <= w.q_ext && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
+#pragma unroll
+          for (int j = 0; j < HALF; j += 4) {
+            if (vec) {
+              reinterpret_cast<float4*>(dst + j)[0] = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+            } else {
+#pragma unroll
+              for (int x = 0; x < 4; ++x)
+                if (q0 + j + x < w.q_ext) dst[j + x] = acc[j + x];
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
+    };
+    auto flush = [&](int64_t g) {
+      const int buf = (int)(g & 1);
+      ok = mbar_wait(&accf[buf], (uint32_t)(g >> 1) & 1, err, 4);
       ok = __all_sync(0xffffffffu, ok);  // tensor-memory loads are warp-collective
       if (!ok) return;
       tc_fence_after();
-      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
+      const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN + half * HALF);
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 8) {
+      for (int c0 = 0; c0 < HALF; c0 += 8) {
         float v[8];
         tmem_ld8(base + (uint32_t)c0, v);
 #pragma unroll
@@ -337,36 +394,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
+      if (g % w.kblocks == w.kblocks - 1) store_tile(g / w.kblocks);
     };
-    for (int kb = 0; kb <= kblocks && ok; ++kb) {
-      if (SPLIT && kb < kblocks) split_stage(kb);
-      if (ok && kb >= 1) flush(kb - 1);
-    }
-    if (ok) {
-      const int p = tile_p + quad * 32 + lane;
-      float* cb = out.c + (int64_t)batch * out.sc;
-      if (p < out.p_ext) {
-        if (!out.swap) {
-#pragma unroll
-          for (int j = 0; j < BN; ++j) {
-            const int q = tile_q + j;
-            if (q < out.q_ext) cb[(int64_t)q * out.ldc + p] = acc[j];
-          }
-        } else {
-          float* dst = cb + (int64_t)p * out.ldc + tile_q;
-          const bool vec = tile_q + BN <= out.q_ext && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0);
-#pragma unroll
-          for (int j = 0; j < BN; j += 4) {
-            if (vec) {
-              reinterpret_cast<float4*>(dst + j)[0] = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-            } else {
-#pragma unroll
-              for (int x = 0; x < 4; ++x)
-                if (tile_q + j + x < out.q_ext) dst[j + x] = acc[j + x];
-            }
-          }
-        }
-      }
+    for (int64_t g = 0; g <= steps && ok; ++g) {
+      if (SPLIT && g < steps) split_stage(g);
+      if (ok && g >= 1) flush(g - 1);
     }
   }
   // no MMA may still write the accumulator when it is freed: the final commit
@@ -477,10 +509,10 @@ bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t kr, int
 }
 
 template <int BN, bool SPLIT>
-cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcOut& o, int64_t p_ext, int64_t q_ext,
-                      int kblocks, int64_t nbatch, int pb, int qb, int* err, cudaStream_t s) {
+cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err, cudaStream_t s) {
   const int bytes = TcSmem<BN>::kBytes;
   static bool attr[64] = {false};  // per device (setting it twice is harmless)
+  static int sms[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
@@ -488,10 +520,13 @@ cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcOut&
     cudaError_t e = cudaFuncSetAttribute(tn_gemm_tc_kernel<BN, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          bytes);
     if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
     attr[dev] = true;
   }
-  dim3 grid((unsigned)((p_ext + 127) / 128), (unsigned)((q_ext + BN - 1) / BN), (unsigned)nbatch);
-  tn_gemm_tc_kernel<BN, SPLIT><<<grid, kTcThreads, bytes, s>>>(mp, mq, o, kblocks, pb, qb, err);
+  // persistent: one CTA per SM (its shared memory admits one)
+  const int64_t grid = w.tiles < sms[dev] ? w.tiles : sms[dev];
+  tn_gemm_tc_kernel<BN, SPLIT><<<(unsigned)grid, kTcThreads, bytes, s>>>(mp, mq, w, err);
   return cudaGetLastError();
 }
 
@@ -513,27 +548,33 @@ cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   const float* Q = static_cast<const float*>(swap ? g.a : g.b);
   const int64_t pe = swap ? g.nr : g.mr, qe = swap ? g.mr : g.nr;
   const int64_t sp = swap ? g.sb : g.sa, sq = swap ? g.sa : g.sb;
-  const int bn = qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
+  const int bn = qe >= 128 ? 128 : qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
   CUtensorMap mp, mq;
   if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn))
     return cudaErrorInvalidValue;
-  TcOut o;
-  o.c = static_cast<float*>(g.c);
-  o.sc = g.sc;
-  o.ldc = g.mr;
-  o.swap = swap ? 1 : 0;
-  o.p_ext = (int32_t)pe;
-  o.q_ext = (int32_t)qe;
-  const int kblocks = (int)((g.kr + kKBlock - 1) / kKBlock);
-  const int pb = sp != 0, qb = sq != 0;
+  TcWork w;
+  w.c = static_cast<float*>(g.c);
+  w.sc = g.sc;
+  w.ldc = g.mr;
+  w.swap = swap ? 1 : 0;
+  w.p_ext = (int32_t)pe;
+  w.q_ext = (int32_t)qe;
+  w.tiles_p = (int32_t)((pe + 127) / 128);
+  w.tiles_q = (int32_t)((qe + bn - 1) / bn);
+  w.kblocks = (int32_t)((g.kr + kKBlock - 1) / kKBlock);
+  w.p_batched = sp != 0;
+  w.q_batched = sq != 0;
+  w.tiles = (int64_t)w.tiles_p * w.tiles_q * g.nbatch;
   if (split) {
-    if (bn == 64) return launch_tc<64, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
-    if (bn == 32) return launch_tc<32, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
-    return launch_tc<16, true>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+    if (bn == 128) return launch_tc<128, true>(mp, mq, w, g.err, s);
+    if (bn == 64) return launch_tc<64, true>(mp, mq, w, g.err, s);
+    if (bn == 32) return launch_tc<32, true>(mp, mq, w, g.err, s);
+    return launch_tc<16, true>(mp, mq, w, g.err, s);
   }
-  if (bn == 64) return launch_tc<64, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
-  if (bn == 32) return launch_tc<32, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
-  return launch_tc<16, false>(mp, mq, o, pe, qe, kblocks, g.nbatch, pb, qb, g.err, s);
+  if (bn == 128) return launch_tc<128, false>(mp, mq, w, g.err, s);
+  if (bn == 64) return launch_tc<64, false>(mp, mq, w, g.err, s);
+  if (bn == 32) return launch_tc<32, false>(mp, mq, w, g.err, s);
+  return launch_tc<16, false>(mp, mq, w, g.err, s);
 }
 
 template <typename real>
