@@ -473,6 +473,48 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   }
 }
 
+// Few outputs and a long sum (the network's closing contractions: a 1 x 2
+// real result over thousands of terms): one CTA per batch entry, every thread
+// accumulates a strided part of each output's sum, then a block reduction.
+template <typename real>
+__global__ void __launch_bounds__(256)
+    tn_gemm_dot_kernel(const real* __restrict__ a, const real* __restrict__ b, real* __restrict__ c, int mr, int nr,
+                       int64_t kr, int64_t sa, int64_t sb, int64_t sc) {
+  constexpr int kMaxOut = 16;
+  __shared__ real part[kMaxOut][8];
+  const int64_t bt = blockIdx.x;
+  const real* A = a + bt * sa;
+  const real* B = b + bt * sb;
+  real acc[kMaxOut];
+#pragma unroll
+  for (int o = 0; o < kMaxOut; ++o) acc[o] = 0;
+  for (int64_t k = threadIdx.x; k < kr; k += blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i >= mr) break;
+      const real x = A[(int64_t)i * kr + k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < nr) acc[i * 4 + j] = fma(x, B[(int64_t)j * kr + k], acc[i * 4 + j]);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 0; o < kMaxOut; ++o) {
+    real v = acc[o];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) part[o][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < mr * nr) {
+    const int i = threadIdx.x / nr, j = threadIdx.x % nr;
+    real v = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += part[i * 4 + j][w];
+    c[bt * sc + (int64_t)j * mr + i] = v;
+  }
+}
+
 // ------------------------------------------------------------------ host side
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
@@ -582,7 +624,9 @@ cudaError_t tn_gemm_simt(const TnGemmArgs& g, cudaStream_t s) {
   const real* A = static_cast<const real*>(g.a);
   const real* B = static_cast<const real*>(g.b);
   real* C = static_cast<real*>(g.c);
-  if (g.mr >= 64 && g.nr >= 64) {
+  if (g.mr <= 4 && g.nr <= 4 && g.kr >= 256 && g.nbatch <= 0x7fffffff) {
+    tn_gemm_dot_kernel<real><<<(unsigned)g.nbatch, 256, 0, s>>>(A, B, C, (int)g.mr, (int)g.nr, g.kr, g.sa, g.sb, g.sc);
+  } else if (g.mr >= 64 && g.nr >= 64) {
     dim3 grid((unsigned)((g.mr + 63) / 64), (unsigned)((g.nr + 63) / 64), (unsigned)g.nbatch);
     tn_gemm_simt_kernel<real, 64, 64, 4, 4><<<grid, 256, 0, s>>>(A, B, C, g.mr, g.nr, g.kr, g.sa, g.sb, g.sc);
   } else {

@@ -88,3 +88,11 @@ def test_gemm_rejects_unsupported_tensor_core_shape():
                                  ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(C.data_ptr()), 8, 8, 6, 0, 0, 0, 1,
                                  ctypes.c_void_p(err.data_ptr()), None)
     assert st == _lib.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_gemm_tiny_output_long_sum(prec):
+    """The closing contraction shape (1 x 2 outputs over 8192 terms) runs on
+    the block-reduction kernel."""
+    got, want, scale = _run("auto" if prec == "c64" else "fp32", prec, 1, 2, 8192, 5, seed=8)
+    assert (got - want).abs().max().item() <= (2e-6 if prec == "c64" else 1e-13) * scale
