@@ -408,7 +408,7 @@ int32_t tedq_tn_profile_read(tedq_tn_plan_t* plan, tedq_tn_profile_t* out);
  * sa, sb, sc: elements between batch entries (0: operand shared by all).
  * precision TEDQ_PREC_C64: float data, mode TEDQ_TN_GEMM_* (TC32 / TF32
  * return TEDQ_ERR_UNSUPPORTED where the tensor-core kernel does not apply:
- * kr a multiple of 4 and >= 8, the larger of mr, nr >= 32, the smaller >= 8,
+ * kr a multiple of 4, the larger of mr, nr >= 32, the smaller >= 8,
  * 16-byte aligned A and B; AUTO then uses FMA); TEDQ_PREC_C128: double data,
  * FP64 FMA.  err_word: a device int32 that the tensor-core kernel sets when
  * one of its bounded waits gives up (required for TC32 / TF32 / AUTO). */

@@ -7,7 +7,8 @@
 //
 // FP32-accurate tensor-core path (complex64 plans): tcgen05.mma kind::tf32
 // with the 3xTF32 split.  Each operand x is split in shared memory into
-// hi = tf32(x) (round to nearest) and lo = tf32(x - hi); the accumulator in
+// hi = tf32(x) (rounded to nearest by two integer operations) and
+// lo = tf32(x - hi); the accumulator in
 // tensor memory receives hi*hi + hi*lo + lo*hi (the dropped lo*lo term and
 // the rounding of lo are below 2^-21 relative).  The tensor cores' own
 // accumulation truncates: each 32-wide K-block is accumulated in a fresh
@@ -107,15 +108,18 @@ __device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand in the canonical 128-byte
-// swizzled layout (8-row atoms of 128 bytes, atoms 1024 bytes apart).
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+// Shared-memory matrix descriptor: K-major operand in the canonical swizzled
+// layout whose rows are KB FP32 values (KB * 4 = 128, 64 or 32 bytes, the
+// swizzle span), 8-row atoms 8 * KB * 4 bytes apart.
+template <int KB>
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  constexpr uint32_t layout = KB == 32 ? 2u : KB == 16 ? 4u : 6u;  // 128-, 64-, 32-byte swizzle
   uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);        // start address
-  d |= (uint64_t)(1) << 16;                        // leading byte offset (unused for K-major swizzled)
-  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // stride byte offset: 8 rows x 128 bytes
-  d |= (uint64_t)1 << 46;                          // descriptor version (sm_100 family)
-  d |= (uint64_t)2 << 61;                          // layout: 128-byte swizzle
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);              // start address
+  d |= (uint64_t)(1) << 16;                              // leading byte offset (unused for K-major swizzled)
+  d |= (uint64_t)(((8 * KB * 4) >> 4) & 0x3FFF) << 32;   // stride byte offset: 8 rows
+  d |= (uint64_t)1 << 46;                                // descriptor version (sm_100 family)
+  d |= (uint64_t)layout << 61;
   return d;
 }
 
@@ -174,25 +178,28 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+// x rounded to the 10 explicit mantissa bits of TF32, to nearest (ties away
+// from zero) with two integer operations: add half of the dropped range to
+// the magnitude bits and clear them.  A carry out of the mantissa raises the
+// exponent, which is the rounded value.  Finite inputs only (the operands are
+// finite whenever the parameters are).
+__device__ __forceinline__ float tf32_round(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 // ------------------------------------------------------------------ tensor-core kernel
 
 constexpr int kTcThreads = 320;  // 10 warps
-constexpr int kKBlock = 32;      // K elements per stage (one 128-byte swizzle row)
 constexpr int kEpiWarps = 8;     // split + epilogue warps (two per tensor-memory lane quadrant)
 
-template <int BN>
+// KB: K elements per stage, one swizzle row (32, or 16 / 8 for short sums)
+template <int BN, int KB>
 struct TcSmem {
-  static constexpr int kA = 128 * kKBlock * 4;  // bytes of one P tile
-  static constexpr int kB = BN * kKBlock * 4;   // bytes of one Q tile
+  static constexpr int kA = 128 * KB * 4;       // bytes of one P tile
+  static constexpr int kB = BN * KB * 4;        // bytes of one Q tile
   static constexpr int kStage = 2 * (kA + kB);  // hi and lo of both
   // as many stages as fit next to the barriers in 200 KB
-  static constexpr int kStages = (200 * 1024) / kStage > 6 ? 6 : (200 * 1024) / kStage;
+  static constexpr int kStages = (200 * 1024) / kStage > 8 ? 8 : (200 * 1024) / kStage;
   static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 512 /* barriers */;
   static_assert(kStages >= 2, "pipeline depth");
   static_assert((3 * kStages + 5) * 8 + 4 <= 512, "barrier region");
@@ -215,11 +222,11 @@ struct TcWork {
 // Persistent: CTA b processes tiles b, b + grid, ...; its producer, MMA
 // issuer and epilogue warps walk the same sequence of (tile, K-block) steps,
 // so the pipeline runs on across tile boundaries.
-template <int BN, bool SPLIT>
+template <int BN, bool SPLIT, int KB>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tn_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_p, const __grid_constant__ CUtensorMap map_q,
                       const TcWork w, int* err) {
-  using S = TcSmem<BN>;
+  using S = TcSmem<BN, KB>;
   constexpr int kStages = S::kStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -278,8 +285,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int kb = (int)(g % w.kblocks);
         unsigned char* st = smem + s * S::kStage;
         mbar_expect_tx(&full[s], S::kA + S::kB);
-        tma_load_3d(st, &map_p, &full[s], kb * kKBlock, tp * 128, w.p_batched ? b : 0);
-        tma_load_3d(st + S::kA, &map_q, &full[s], kb * kKBlock, tq * BN, w.q_batched ? b : 0);
+        tma_load_3d(st, &map_p, &full[s], kb * KB, tp * 128, w.p_batched ? b : 0);
+        tma_load_3d(st + S::kA, &map_q, &full[s], kb * KB, tq * BN, w.q_batched ? b : 0);
         issued = g + 1;
       }
       // every issued copy has landed before the CTA may exit (immediate on the
@@ -302,11 +309,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const uint32_t a_hi = st, b_hi = st + S::kA, a_lo = st + S::kA + S::kB, b_lo = a_lo + S::kA;
         const uint32_t d = tmem + (uint32_t)(buf * BN);
 #pragma unroll
-        for (int k = 0; k < kKBlock / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
-          mma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, k > 0 ? 1u : 0u);
+        for (int k = 0; k < KB / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
+          mma_tf32(d, smem_desc<KB>(a_hi + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc, k > 0 ? 1u : 0u);
           if (SPLIT) {
-            mma_tf32(d, smem_desc_sw128(a_hi + 32 * k), smem_desc_sw128(b_lo + 32 * k), idesc, 1u);
-            mma_tf32(d, smem_desc_sw128(a_lo + 32 * k), smem_desc_sw128(b_hi + 32 * k), idesc, 1u);
+            mma_tf32(d, smem_desc<KB>(a_hi + 32 * k), smem_desc<KB>(b_lo + 32 * k), idesc, 1u);
+            mma_tf32(d, smem_desc<KB>(a_lo + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc, 1u);
           }
         }
         mma_commit(&empty[s]);    // frees the stage when these MMAs have read it
@@ -337,10 +344,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll 4
       for (int i = t; i < n4; i += 32 * kEpiWarps) {
         float4 x = hi[i], h, l;
-        h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
-        h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
-        h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
-        h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+        h.x = tf32_round(x.x); l.x = tf32_round(x.x - h.x);
+        h.y = tf32_round(x.y); l.y = tf32_round(x.y - h.y);
+        h.z = tf32_round(x.z); l.z = tf32_round(x.z - h.z);
+        h.w = tf32_round(x.w); l.w = tf32_round(x.w - h.w);
         hi[i] = h;
         lo[i] = l;
       }
@@ -535,31 +542,34 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-// [batch][rows][kr] FP32, box [1][box_rows][32], 128-byte swizzle; rows and
-// K beyond the extents read as zero
+// [batch][rows][kr] FP32, box [1][box_rows][kb], kb * 4-byte swizzle; rows
+// and K beyond the extents read as zero
 bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t kr, int64_t batch, int64_t bstride,
-              int box_rows) {
+              int box_rows, int kb) {
   EncodeTiled enc = encode_fn();
   if (!enc) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)kr, (cuuint64_t)rows, (cuuint64_t)(bstride ? batch : 1)};
   const cuuint64_t strides[2] = {(cuuint64_t)kr * 4, (cuuint64_t)(bstride ? bstride : rows * kr) * 4};
-  const cuuint32_t box[3] = {32, (cuuint32_t)box_rows, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)kb, (cuuint32_t)box_rows, 1};
+  const CUtensorMapSwizzle sw = kb == 32 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : kb == 16 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                           : CU_TENSOR_MAP_SWIZZLE_32B;
   const cuuint32_t estr[3] = {1, 1, 1};
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN, bool SPLIT>
+template <int BN, bool SPLIT, int KB>
 cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err, cudaStream_t s) {
-  const int bytes = TcSmem<BN>::kBytes;
+  const int bytes = TcSmem<BN, KB>::kBytes;
   static bool attr[64] = {false};  // per device (setting it twice is harmless)
   static int sms[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   if (!attr[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(tn_gemm_tc_kernel<BN, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tn_gemm_tc_kernel<BN, SPLIT, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          bytes);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
@@ -568,8 +578,30 @@ cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcWork
   }
   // persistent: one CTA per SM (its shared memory admits one)
   const int64_t grid = w.tiles < sms[dev] ? w.tiles : sms[dev];
-  tn_gemm_tc_kernel<BN, SPLIT><<<(unsigned)grid, kTcThreads, bytes, s>>>(mp, mq, w, err);
+  tn_gemm_tc_kernel<BN, SPLIT, KB><<<(unsigned)grid, kTcThreads, bytes, s>>>(mp, mq, w, err);
   return cudaGetLastError();
+}
+
+template <int BN, bool SPLIT>
+cudaError_t dispatch_kb(int kb, const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err,
+                        cudaStream_t s) {
+  if (kb == 8) return launch_tc<BN, SPLIT, 8>(mp, mq, w, err, s);
+  if (kb == 16) return launch_tc<BN, SPLIT, 16>(mp, mq, w, err, s);
+  return launch_tc<BN, SPLIT, 32>(mp, mq, w, err, s);
+}
+
+template <bool SPLIT>
+cudaError_t dispatch_split(int bn, int kb, const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err,
+                           cudaStream_t s) {
+  if (bn == 128) return dispatch_kb<128, SPLIT>(kb, mp, mq, w, err, s);
+  if (bn == 64) return dispatch_kb<64, SPLIT>(kb, mp, mq, w, err, s);
+  if (bn == 32) return dispatch_kb<32, SPLIT>(kb, mp, mq, w, err, s);
+  return dispatch_kb<16, SPLIT>(kb, mp, mq, w, err, s);
+}
+
+cudaError_t dispatch_bn(int bn, bool split, int kb, const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w,
+                        int* err, cudaStream_t s) {
+  return split ? dispatch_split<true>(bn, kb, mp, mq, w, err, s) : dispatch_split<false>(bn, kb, mp, mq, w, err, s);
 }
 
 }  // namespace
@@ -578,7 +610,7 @@ bool tn_gemm_tc_supported(const TnGemmArgs& g) {
   // FP32 rows of kr reals: 16-byte TMA strides and bases; the P side fills a
   // 128-row tile to at least a quarter, the Q side at least 8 columns
   const int64_t P = g.mr >= g.nr ? g.mr : g.nr, Q = g.mr >= g.nr ? g.nr : g.mr;
-  return g.kr % 4 == 0 && g.kr >= 8 && P >= 32 && Q >= 8 && g.nbatch <= 65535 &&
+  return g.kr % 4 == 0 && g.kr >= 4 && P >= 32 && Q >= 8 && g.nbatch <= 65535 &&
          (reinterpret_cast<uintptr_t>(g.a) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.b) & 15) == 0 &&
          (g.sa * 4) % 16 == 0 && (g.sb * 4) % 16 == 0 && encode_fn() != nullptr;
 }
@@ -591,8 +623,11 @@ cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   const int64_t pe = swap ? g.nr : g.mr, qe = swap ? g.mr : g.nr;
   const int64_t sp = swap ? g.sb : g.sa, sq = swap ? g.sa : g.sb;
   const int bn = qe >= 128 ? 128 : qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
+  // K per stage: one swizzle row of 32 values, or 16 / 8 for short sums (no
+  // zero-filled MMAs)
+  const int kb = g.kr <= 8 ? 8 : g.kr <= 16 ? 16 : 32;
   CUtensorMap mp, mq;
-  if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn))
+  if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128, kb) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn, kb))
     return cudaErrorInvalidValue;
   TcWork w;
   w.c = static_cast<float*>(g.c);
@@ -603,20 +638,11 @@ cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   w.q_ext = (int32_t)qe;
   w.tiles_p = (int32_t)((pe + 127) / 128);
   w.tiles_q = (int32_t)((qe + bn - 1) / bn);
-  w.kblocks = (int32_t)((g.kr + kKBlock - 1) / kKBlock);
+  w.kblocks = (int32_t)((g.kr + kb - 1) / kb);
   w.p_batched = sp != 0;
   w.q_batched = sq != 0;
   w.tiles = (int64_t)w.tiles_p * w.tiles_q * g.nbatch;
-  if (split) {
-    if (bn == 128) return launch_tc<128, true>(mp, mq, w, g.err, s);
-    if (bn == 64) return launch_tc<64, true>(mp, mq, w, g.err, s);
-    if (bn == 32) return launch_tc<32, true>(mp, mq, w, g.err, s);
-    return launch_tc<16, true>(mp, mq, w, g.err, s);
-  }
-  if (bn == 128) return launch_tc<128, false>(mp, mq, w, g.err, s);
-  if (bn == 64) return launch_tc<64, false>(mp, mq, w, g.err, s);
-  if (bn == 32) return launch_tc<32, false>(mp, mq, w, g.err, s);
-  return launch_tc<16, false>(mp, mq, w, g.err, s);
+  return dispatch_bn(bn, split, kb, mp, mq, w, g.err, s);
 }
 
 template <typename real>

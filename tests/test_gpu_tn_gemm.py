@@ -4,7 +4,8 @@ C ABI: the tcgen05 tensor-core kernel with the 3xTF32 split (FP32 accuracy)
 and with one TF32 product, the FP32 and FP64 FMA kernels.  Shapes cover the
 6x6-lattice contractions (both orientations: the larger side fills the
 128-row tiles), partial tiles in every dimension, K not a multiple of the
-32-element stage, shared (unbatched) operands and the error word.
+stage's K-block (8, 16 or 32 elements with 32-, 64- and 128-byte swizzles),
+shared (unbatched) operands and the error word.
 
 Tolerance: |C - C64| <= tol * sqrt(kr) * max|A| * max|B| with tol = 2e-6
 (3xTF32, FP32), 2e-3 (TF32), 1e-13 (FP64)."""
@@ -26,7 +27,8 @@ MODES = {"fp32": 0, "tc32": 1, "tf32": 2, "auto": 3}
 # (mr, nr, kr) of the 6x6x8 lattice's large contractions, then edge cases
 SHAPES = [(64, 128, 8), (32, 256, 8), (64, 128, 16), (128, 256, 64), (64, 128, 256), (64, 512, 16),
           (128, 1024, 32), (128, 1024, 128), (256, 512, 256), (32, 256, 512),
-          (200, 40, 12), (40, 200, 44), (130, 17, 36), (512, 8, 100), (96, 96, 4 * 33)]
+          (200, 40, 12), (40, 200, 44), (130, 17, 36), (512, 8, 100), (96, 96, 4 * 33), (64, 96, 4),
+          (128, 64, 12), (300, 24, 16)]
 
 
 def _run(mode, prec, mr, nr, kr, nbatch, shared_a=False, shared_b=False, seed=0):
@@ -84,6 +86,7 @@ def test_gemm_rejects_unsupported_tensor_core_shape():
     A = torch.zeros(8, 6, device=DEV)
     C = torch.zeros(8, 8, device=DEV)
     err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    # kr = 6: rows of 24 bytes cannot be TMA-strided (16-byte multiples)
     st = _lib.lib().tedq_tn_gemm(_lib.PREC_C64, MODES["tc32"], ctypes.c_void_p(A.data_ptr()),
                                  ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(C.data_ptr()), 8, 8, 6, 0, 0, 0, 1,
                                  ctypes.c_void_p(err.data_ptr()), None)
