@@ -17,16 +17,16 @@
 // for long K.  One CTA computes a 128-row
 // tile of the larger side (the "P" operand) against a BN-column tile of the
 // other ("Q"), BN in {16, 32, 64, 128}; persistent CTAs (one per SM) walk
-// their tiles with the pipeline running on across tile boundaries; ten warps:
+// their tiles with the pipeline running on across tile boundaries; warps:
 //   warp 0     TMA producer: 3-D tensor maps [batch][rows][k], 128-byte
 //              swizzle, boxes of 32 K-elements (one swizzle row);
 //   warp 1     allocates the tensor-memory accumulator and issues the MMAs
 //              (one thread), commits each stage back to the producer;
-//   warps 2-9  split each landed stage into hi/lo tiles (element-wise on the
+//   warps 2-   split each landed stage into hi/lo tiles (element-wise on the
 //              swizzled image, so no address arithmetic), add each K-block's
-//              partial sum from tensor memory (tcgen05.ld; two warps per
-//              32-lane quadrant, half of the columns each) into registers,
-//              and store C after a tile's last K-block.
+//              partial sum from tensor memory (tcgen05.ld; four warps per
+//              32-lane quadrant for BN >= 32, a quarter of the columns each)
+//              into registers, and store C after a tile's last K-block.
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by the root kernel, which then returns NaN) and the CTA drains
 // and frees its tensor memory before returning.
@@ -189,8 +189,14 @@ __device__ __forceinline__ float tf32_round(float x) {
 
 // ------------------------------------------------------------------ tensor-core kernel
 
-constexpr int kTcThreads = 320;  // 10 warps
-constexpr int kEpiWarps = 8;     // split + epilogue warps (two per tensor-memory lane quadrant)
+// Split + epilogue warps: CG per tensor-memory lane quadrant, each owning
+// BN / CG accumulator columns (at least 8); two more warps (TMA, MMA).
+template <int BN>
+struct TcWarps {
+  static constexpr int CG = BN >= 32 ? 4 : BN / 8;
+  static constexpr int kEpi = 4 * CG;
+  static constexpr int kThreads = 32 * (2 + kEpi);
+};
 
 // KB: K elements per stage, one swizzle row (32, or 16 / 8 for short sums)
 template <int BN, int KB>
@@ -223,7 +229,7 @@ struct TcWork {
 // issuer and epilogue warps walk the same sequence of (tile, K-block) steps,
 // so the pipeline runs on across tile boundaries.
 template <int BN, bool SPLIT, int KB>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
     tn_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_p, const __grid_constant__ CUtensorMap map_q,
                       const TcWork w, int* err) {
   using S = TcSmem<BN, KB>;
@@ -254,12 +260,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&split[s], SPLIT ? kEpiWarps : 1);
+      mbar_init(&split[s], SPLIT ? TcWarps<BN>::kEpi : 1);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], kEpiWarps);
+      mbar_init(&acce[b], TcWarps<BN>::kEpi);
     }
     mbar_init(done, 1);
     fence_proxy_async();
@@ -326,9 +332,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // partial sum (tensor memory: this warp's 32-lane quadrant, half of the
     // columns) into FP32 registers with round-to-nearest additions; store a
     // tile after its last K-block
-    constexpr int HALF = BN / 2;
-    const int t = threadIdx.x - 64;  // 0..255
-    const int quad = warp & 3, half = (warp - 2) >> 2;
+    constexpr int kEpiWarps = TcWarps<BN>::kEpi;
+    constexpr int HALF = BN / TcWarps<BN>::CG;  // accumulator columns of this warp
+    const int t = threadIdx.x - 64;  // 0 .. 32 * kEpiWarps - 1
+    const int quad = warp & 3, half = (warp - 2) >> 2;  // lane quadrant, column group
     float acc[HALF];
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
@@ -578,7 +585,7 @@ cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcWork
   }
   // persistent: one CTA per SM (its shared memory admits one)
   const int64_t grid = w.tiles < sms[dev] ? w.tiles : sms[dev];
-  tn_gemm_tc_kernel<BN, SPLIT, KB><<<(unsigned)grid, kTcThreads, bytes, s>>>(mp, mq, w, err);
+  tn_gemm_tc_kernel<BN, SPLIT, KB><<<(unsigned)grid, TcWarps<BN>::kThreads, bytes, s>>>(mp, mq, w, err);
   return cudaGetLastError();
 }
 
