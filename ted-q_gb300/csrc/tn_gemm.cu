@@ -36,6 +36,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "tn_gemm.cuh"
 
@@ -74,18 +75,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: about half a second of polling, then the error word is set
-// and false returned.  Once any CTA has set the word, the others give up
-// their waits at the next check instead of polling to their own limit.
+// Bounded wait: polls try_wait (which itself suspends the thread for a short
+// time when the phase is not complete), first without sleeping -- the
+// pipeline's hand-offs sit on the critical path -- then with short sleeps,
+// for about a second in all; then the error word is set and false returned.
+// Once any CTA has set the word, the others give up their waits at the next
+// check instead of polling to their own limit.
 constexpr uint32_t kWaitTries = 1u << 21;
+constexpr uint32_t kSpinTries = 1u << 14;
 
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code, bool bail = true) {
   for (uint32_t t = 0; t < kWaitTries; ++t) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (t > 64) {
-      __nanosleep(t < 4096 ? 32 : 256);
-      if (bail && (t & 1023) == 0 && *(volatile int*)err != 0) return false;
-    }
+    if (t > kSpinTries) __nanosleep(256);
+    if (bail && (t & 1023) == 1023 && *(volatile int*)err != 0) return false;
   }
   atomicExch(err, code);
   return false;
@@ -198,17 +201,26 @@ struct TcWarps {
   static constexpr int kThreads = 32 * (2 + kEpi);
 };
 
-// KB: K elements per stage, one swizzle row (32, or 16 / 8 for short sums)
-template <int BN, int KB>
+// KB: K elements per stage, one swizzle row (32, or 16 / 8 for short sums).
+// Two rings: load stages (the P and Q tiles as TMA writes them) and, with the
+// 3xTF32 split, operand slots (hi and lo of both, read by the MMAs).  A load
+// stage is released as soon as the split has read it, so the loads in flight
+// do not wait for the MMAs; without the split the MMAs read the load stages.
+template <int BN, int KB, bool SPLIT>
 struct TcSmem {
   static constexpr int kA = 128 * KB * 4;       // bytes of one P tile
   static constexpr int kB = BN * KB * 4;        // bytes of one Q tile
-  static constexpr int kStage = 2 * (kA + kB);  // hi and lo of both
-  // as many stages as fit next to the barriers in 200 KB
-  static constexpr int kStages = (200 * 1024) / kStage > 8 ? 8 : (200 * 1024) / kStage;
-  static constexpr int kBytes = kStages * kStage + 1024 /* alignment */ + 512 /* barriers */;
+  static constexpr int kLoad = kA + kB;         // one load stage
+  static constexpr int kOp = SPLIT ? 2 * kLoad : 0;  // one operand slot (hi, lo)
+  static constexpr int kSlots = SPLIT ? 2 : 0;
+  static constexpr int kBudget = 200 * 1024 - kSlots * kOp;
+  // as many load stages as fit next to the barriers in 200 KB
+  static constexpr int kStages = kBudget / kLoad > 8 ? 8 : kBudget / kLoad;
+  static constexpr int kOpBase = kStages * kLoad;
+  static constexpr int kBarBase = kOpBase + kSlots * kOp;
+  static constexpr int kBytes = kBarBase + 1024 /* alignment */ + 512 /* barriers */;
   static_assert(kStages >= 2, "pipeline depth");
-  static_assert((3 * kStages + 5) * 8 + 4 <= 512, "barrier region");
+  static_assert((2 * kStages + 2 * 2 + 5) * 8 + 4 <= 512, "barrier region");
 };
 
 // Work of one launch: tiles of 128 P-rows x BN Q-columns of every batch entry,
@@ -232,16 +244,19 @@ template <int BN, bool SPLIT, int KB>
 __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
     tn_gemm_tc_kernel(const __grid_constant__ CUtensorMap map_p, const __grid_constant__ CUtensorMap map_q,
                       const TcWork w, int* err) {
-  using S = TcSmem<BN, KB>;
+  using S = TcSmem<BN, KB, SPLIT>;
   constexpr int kStages = S::kStages;
+  constexpr int kSlots = S::kSlots > 0 ? S::kSlots : 1;  // operand slots (used with the split only)
+  constexpr int kEpiWarps = TcWarps<BN>::kEpi;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * S::kStage);  // TMA landed
-  uint64_t* split = full + kStages;                                          // hi/lo written
-  uint64_t* empty = split + kStages;                                         // MMAs of the stage done
-  uint64_t* accf = empty + kStages;   // [2] K-block partial complete in accumulator buffer b
-  uint64_t* acce = accf + 2;          // [2] accumulator buffer b read back
-  uint64_t* done = acce + 2;          // every MMA complete
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::kBarBase);  // [kStages] TMA landed
+  uint64_t* lfree = full + kStages;   // [kStages] load stage free (read by the split, or by the MMAs)
+  uint64_t* opready = lfree + kStages;  // [2] operand slot written (split)
+  uint64_t* opfree = opready + 2;       // [2] operand slot's MMAs complete
+  uint64_t* accf = opfree + 2;          // [2] K-block partial complete in accumulator buffer b
+  uint64_t* acce = accf + 2;            // [2] accumulator buffer b read back
+  uint64_t* done = acce + 2;            // every MMA complete
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // two accumulator buffers of BN columns: the MMAs of a K-block write one
@@ -260,12 +275,13 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&split[s], SPLIT ? TcWarps<BN>::kEpi : 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&lfree[s], SPLIT ? kEpiWarps : 1);
     }
     for (int b = 0; b < 2; ++b) {
+      mbar_init(&opready[b], kEpiWarps);
+      mbar_init(&opfree[b], 1);
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], TcWarps<BN>::kEpi);
+      mbar_init(&acce[b], kEpiWarps);
     }
     mbar_init(done, 1);
     fence_proxy_async();
@@ -284,12 +300,12 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
       int64_t issued = 0;  // steps whose loads were issued
       for (int64_t g = 0; g < steps && ok; ++g) {
         const int s = (int)(g % kStages);
-        if (g >= kStages) ok = mbar_wait(&empty[s], (uint32_t)((g / kStages) - 1) & 1, err, 1);
+        if (g >= kStages) ok = mbar_wait(&lfree[s], (uint32_t)((g / kStages) - 1) & 1, err, 1);
         if (!ok) break;
         int tp, tq, b;
         tile_of(g / w.kblocks, tp, tq, b);
         const int kb = (int)(g % w.kblocks);
-        unsigned char* st = smem + s * S::kStage;
+        unsigned char* st = smem + s * S::kLoad;
         mbar_expect_tx(&full[s], S::kA + S::kB);
         tma_load_3d(st, &map_p, &full[s], kb * KB, tp * 128, w.p_batched ? b : 0);
         tma_load_3d(st + S::kA, &map_q, &full[s], kb * KB, tq * BN, w.q_batched ? b : 0);
@@ -304,15 +320,23 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BN);
       for (int64_t g = 0; g < steps && ok; ++g) {
-        const int s = (int)(g % kStages), buf = (int)(g & 1);
-        const uint32_t par = (uint32_t)(g / kStages) & 1;
+        const int buf = (int)(g & 1);
         if (g >= 2) ok = mbar_wait(&acce[buf], (uint32_t)((g >> 1) - 1) & 1, err, 7);  // buffer read back
         if (!ok) break;
-        ok = SPLIT ? mbar_wait(&split[s], par, err, 2) : mbar_wait(&full[s], par, err, 2);
+        uint32_t a_hi, b_hi, a_lo = 0, b_lo = 0;
+        if (SPLIT) {
+          const int slot = (int)(g % kSlots);
+          ok = mbar_wait(&opready[slot], (uint32_t)(g / kSlots) & 1, err, 2);
+          const uint32_t op = smem_u32(smem + S::kOpBase + slot * S::kOp);
+          a_hi = op, b_hi = op + S::kA, a_lo = op + S::kA + S::kB, b_lo = a_lo + S::kA;
+        } else {
+          const int s = (int)(g % kStages);
+          ok = mbar_wait(&full[s], (uint32_t)(g / kStages) & 1, err, 2);
+          const uint32_t st = smem_u32(smem + s * S::kLoad);
+          a_hi = st, b_hi = st + S::kA;
+        }
         if (!ok) break;
         tc_fence_after();
-        const uint32_t st = smem_u32(smem + s * S::kStage);
-        const uint32_t a_hi = st, b_hi = st + S::kA, a_lo = st + S::kA + S::kB, b_lo = a_lo + S::kA;
         const uint32_t d = tmem + (uint32_t)(buf * BN);
 #pragma unroll
         for (int k = 0; k < KB / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
@@ -322,17 +346,17 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
             mma_tf32(d, smem_desc<KB>(a_lo + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc, 1u);
           }
         }
-        mma_commit(&empty[s]);    // frees the stage when these MMAs have read it
+        // frees what these MMAs read once they have read it
+        mma_commit(SPLIT ? &opfree[g % kSlots] : &lfree[g % kStages]);
         mma_commit(&accf[buf]);   // the K-block's partial sum is ready
       }
       mma_commit(done);
     }
   } else {
-    // warps 2-9: split each landed stage into hi / lo, and add each K-block's
-    // partial sum (tensor memory: this warp's 32-lane quadrant, half of the
-    // columns) into FP32 registers with round-to-nearest additions; store a
-    // tile after its last K-block
-    constexpr int kEpiWarps = TcWarps<BN>::kEpi;
+    // split + epilogue warps: split each landed stage into hi / lo operand
+    // tiles, and add each K-block's partial sum (tensor memory: this warp's
+    // 32-lane quadrant, its group of columns) into FP32 registers with
+    // round-to-nearest additions; store a tile after its last K-block
     constexpr int HALF = BN / TcWarps<BN>::CG;  // accumulator columns of this warp
     const int t = threadIdx.x - 64;  // 0 .. 32 * kEpiWarps - 1
     const int quad = warp & 3, half = (warp - 2) >> 2;  // lane quadrant, column group
@@ -340,17 +364,19 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
     auto split_stage = [&](int64_t g) {
-      const int s = (int)(g % kStages);
+      const int s = (int)(g % kStages), slot = (int)(g % kSlots);
       ok = mbar_wait(&full[s], (uint32_t)(g / kStages) & 1, err, 3);
+      // the operand slot's previous MMAs (step g - 2) have read it
+      if (ok && g >= kSlots) ok = mbar_wait(&opfree[slot], (uint32_t)((g / kSlots) - 1) & 1, err, 8);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) return;
-      unsigned char* st = smem + s * S::kStage;
-      float4* hi = reinterpret_cast<float4*>(st);                  // P tile then Q tile
-      float4* lo = reinterpret_cast<float4*>(st + S::kA + S::kB);  // same order
-      constexpr int n4 = (S::kA + S::kB) / 16;
+      const float4* raw = reinterpret_cast<const float4*>(smem + s * S::kLoad);  // P tile then Q tile
+      float4* hi = reinterpret_cast<float4*>(smem + S::kOpBase + slot * S::kOp);  // same order
+      float4* lo = reinterpret_cast<float4*>(smem + S::kOpBase + slot * S::kOp + S::kLoad);
+      constexpr int n4 = S::kLoad / 16;
 #pragma unroll 4
       for (int i = t; i < n4; i += 32 * kEpiWarps) {
-        float4 x = hi[i], h, l;
+        float4 x = raw[i], h, l;
         h.x = tf32_round(x.x); l.x = tf32_round(x.x - h.x);
         h.y = tf32_round(x.y); l.y = tf32_round(x.y - h.y);
         h.z = tf32_round(x.z); l.z = tf32_round(x.z - h.z);
@@ -360,7 +386,10 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
       }
       fence_proxy_async();  // generic-proxy writes -> visible to the tensor cores
       __syncwarp();
-      if (lane == 0) mbar_arrive(&split[s]);
+      if (lane == 0) {
+        mbar_arrive(&lfree[s]);        // the load stage may be refilled
+        mbar_arrive(&opready[slot]);   // the MMAs may read the operands
+      }
     };
     auto store_tile = [&](int64_t i) {
       int tp, tq, b;
@@ -569,7 +598,7 @@ bool make_map(CUtensorMap* map, const float* base, int64_t rows, int64_t kr, int
 
 template <int BN, bool SPLIT, int KB>
 cudaError_t launch_tc(const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err, cudaStream_t s) {
-  const int bytes = TcSmem<BN, KB>::kBytes;
+  const int bytes = TcSmem<BN, KB, SPLIT>::kBytes;
   static bool attr[64] = {false};  // per device (setting it twice is harmless)
   static int sms[64] = {0};
   int dev = 0;
@@ -632,7 +661,14 @@ cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   const int bn = qe >= 128 ? 128 : qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
   // K per stage: one swizzle row of 32 values, or 16 / 8 for short sums (no
   // zero-filled MMAs)
-  const int kb = g.kr <= 8 ? 8 : g.kr <= 16 ? 16 : 32;
+  // TEDQ_GB300_TN_GEMM_KB (8, 16 or 32) caps it: a tuning knob for measurements
+  static const int kb_cap = [] {
+    const char* e = getenv("TEDQ_GB300_TN_GEMM_KB");
+    const int v = e ? atoi(e) : 32;
+    return v == 8 || v == 16 ? v : 32;
+  }();
+  int kb = g.kr <= 8 ? 8 : g.kr <= 16 ? 16 : 32;
+  kb = kb < kb_cap ? kb : kb_cap;
   CUtensorMap mp, mq;
   if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128, kb) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn, kb))
     return cudaErrorInvalidValue;
