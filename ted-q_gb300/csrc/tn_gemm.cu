@@ -11,10 +11,10 @@
 // lo = tf32(x - hi); the accumulator in
 // tensor memory receives hi*hi + hi*lo + lo*hi (the dropped lo*lo term and
 // the rounding of lo are below 2^-21 relative).  The tensor cores' own
-// accumulation truncates: each 32-wide K-block is accumulated in a fresh
-// tensor-memory buffer (two, alternating) and the blocks are summed in FP32
-// registers with round-to-nearest, which keeps the result at FP32 accuracy
-// for long K.  One CTA computes a 128-row
+// accumulation truncates: each group of 64 K-elements is accumulated in a
+// fresh tensor-memory buffer (four, in turn) and the groups are summed in
+// FP32 registers with round-to-nearest, which keeps the result at FP32
+// accuracy for long K.  One CTA computes a 128-row
 // tile of the larger side (the "P" operand) against a BN-column tile of the
 // other ("Q"), BN in {16, 32, 64, 128}; persistent CTAs (one per SM) walk
 // their tiles with the pipeline running on across tile boundaries; warps:
@@ -220,7 +220,7 @@ struct TcSmem {
   static constexpr int kBarBase = kOpBase + kSlots * kOp;
   static constexpr int kBytes = kBarBase + 1024 /* alignment */ + 512 /* barriers */;
   static_assert(kStages >= 2, "pipeline depth");
-  static_assert((2 * kStages + 2 * 2 + 5) * 8 + 4 <= 512, "barrier region");
+  static_assert((2 * kStages + 2 * 2 + 2 * 4 + 1) * 8 + 4 <= 512, "barrier region");
 };
 
 // Work of one launch: tiles of 128 P-rows x BN Q-columns of every batch entry,
@@ -248,22 +248,31 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
   constexpr int kStages = S::kStages;
   constexpr int kSlots = S::kSlots > 0 ? S::kSlots : 1;  // operand slots (used with the split only)
   constexpr int kEpiWarps = TcWarps<BN>::kEpi;
+  // accumulator buffers (512 tensor-memory columns at most, one CTA per SM)
+  // and K-blocks accumulated per buffer before the epilogue adds them up in
+  // FP32 (64 K-elements: the tensor cores' truncating accumulation stays
+  // short)
+  constexpr int kBufs = 512 / BN < 4 ? 512 / BN : 4;
+  constexpr int kGroup = 64 / KB;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S::kBarBase);  // [kStages] TMA landed
   uint64_t* lfree = full + kStages;   // [kStages] load stage free (read by the split, or by the MMAs)
   uint64_t* opready = lfree + kStages;  // [2] operand slot written (split)
   uint64_t* opfree = opready + 2;       // [2] operand slot's MMAs complete
-  uint64_t* accf = opfree + 2;          // [2] K-block partial complete in accumulator buffer b
-  uint64_t* acce = accf + 2;            // [2] accumulator buffer b read back
-  uint64_t* done = acce + 2;            // every MMA complete
+  uint64_t* accf = opfree + 2;          // [kBufs] group partial complete in accumulator buffer b
+  uint64_t* acce = accf + kBufs;        // [kBufs] accumulator buffer b read back
+  uint64_t* done = acce + kBufs;        // every MMA complete
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // two accumulator buffers of BN columns: the MMAs of a K-block write one
-  // while the epilogue warps add the other into FP32 registers
-  constexpr uint32_t kCols = 2 * BN < 32 ? 32 : 2 * BN;
+  // kBufs accumulator buffers of BN columns: the MMAs of a group of K-blocks
+  // write one while the epilogue warps add finished ones into FP32 registers
+  constexpr uint32_t kCols = kBufs * BN < 32 ? 32 : kBufs * BN;
   const int64_t my_tiles = w.tiles > blockIdx.x ? (w.tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const int64_t steps = my_tiles * w.kblocks;
+  // groups of up to kGroup K-blocks per accumulator buffer; a tile's last
+  // group may be shorter.  Global group id of step g: tile * groups + kb / kGroup
+  const int groups = (w.kblocks + kGroup - 1) / kGroup;
   auto tile_of = [&](int64_t i, int& tp, int& tq, int& b) {
     const int64_t t = blockIdx.x + i * gridDim.x;
     tp = (int)(t % w.tiles_p);
@@ -280,6 +289,8 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
     for (int b = 0; b < 2; ++b) {
       mbar_init(&opready[b], kEpiWarps);
       mbar_init(&opfree[b], 1);
+    }
+    for (int b = 0; b < kBufs; ++b) {
       mbar_init(&accf[b], 1);
       mbar_init(&acce[b], kEpiWarps);
     }
@@ -320,8 +331,12 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BN);
       for (int64_t g = 0; g < steps && ok; ++g) {
-        const int buf = (int)(g & 1);
-        if (g >= 2) ok = mbar_wait(&acce[buf], (uint32_t)((g >> 1) - 1) & 1, err, 7);  // buffer read back
+        const int kb = (int)(g % w.kblocks);
+        const int64_t gid = (g / w.kblocks) * groups + kb / kGroup;
+        const int buf = (int)(gid % kBufs);
+        const bool first = kb % kGroup == 0, last = kb % kGroup == kGroup - 1 || kb == w.kblocks - 1;
+        if (first && gid >= kBufs)  // buffer read back
+          ok = mbar_wait(&acce[buf], (uint32_t)((gid / kBufs) - 1) & 1, err, 7);
         if (!ok) break;
         uint32_t a_hi, b_hi, a_lo = 0, b_lo = 0;
         if (SPLIT) {
@@ -340,7 +355,8 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
         const uint32_t d = tmem + (uint32_t)(buf * BN);
 #pragma unroll
         for (int k = 0; k < KB / 8; ++k) {  // K = 8 per MMA: 32 bytes along the swizzle row
-          mma_tf32(d, smem_desc<KB>(a_hi + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc, k > 0 ? 1u : 0u);
+          mma_tf32(d, smem_desc<KB>(a_hi + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc,
+                   (first && k == 0) ? 0u : 1u);
           if (SPLIT) {
             mma_tf32(d, smem_desc<KB>(a_hi + 32 * k), smem_desc<KB>(b_lo + 32 * k), idesc, 1u);
             mma_tf32(d, smem_desc<KB>(a_lo + 32 * k), smem_desc<KB>(b_hi + 32 * k), idesc, 1u);
@@ -348,7 +364,7 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
         }
         // frees what these MMAs read once they have read it
         mma_commit(SPLIT ? &opfree[g % kSlots] : &lfree[g % kStages]);
-        mma_commit(&accf[buf]);   // the K-block's partial sum is ready
+        if (last) mma_commit(&accf[buf]);   // the group's partial sum is ready
       }
       mma_commit(done);
     }
@@ -420,9 +436,10 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
 #pragma unroll
       for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
     };
-    auto flush = [&](int64_t g) {
-      const int buf = (int)(g & 1);
-      ok = mbar_wait(&accf[buf], (uint32_t)(g >> 1) & 1, err, 4);
+    // adds group gid of tile `tile` (buffer gid % kBufs) into the registers
+    auto flush = [&](int64_t gid, int64_t tile, bool tile_end) {
+      const int buf = (int)(gid % kBufs);
+      ok = mbar_wait(&accf[buf], (uint32_t)(gid / kBufs) & 1, err, 4);
       ok = __all_sync(0xffffffffu, ok);  // tensor-memory loads are warp-collective
       if (!ok) return;
       tc_fence_after();
@@ -437,11 +454,16 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[buf]);
-      if (g % w.kblocks == w.kblocks - 1) store_tile(g / w.kblocks);
+      if (tile_end) store_tile(tile);
     };
     for (int64_t g = 0; g <= steps && ok; ++g) {
       if (SPLIT && g < steps) split_stage(g);
-      if (ok && g >= 1) flush(g - 1);
+      if (ok && g >= 1) {  // step g - 1 closed a group: add it
+        const int64_t h = g - 1;
+        const int kb = (int)(h % w.kblocks);
+        if (kb % kGroup == kGroup - 1 || kb == w.kblocks - 1)
+          flush((h / w.kblocks) * groups + kb / kGroup, h / w.kblocks, kb == w.kblocks - 1);
+      }
     }
   }
   // no MMA may still write the accumulator when it is freed: the final commit
