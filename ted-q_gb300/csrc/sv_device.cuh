@@ -1166,7 +1166,7 @@ struct BwdPass {
   S* tp;
   S* tl;
   C (*mats)[4];
-  double* gacc;
+  real* gacc;  // per-warp gradient partials (the warp sums, in the state's precision)
   C* sp;
   C* sl;
   double* grad_acc;
@@ -1179,7 +1179,7 @@ struct BwdPass {
   Regs<real, R> a;
   Regs<real, R> l;
 
-  __device__ __forceinline__ BwdPass(const PassParams& P_, S* smem, C (*mats_)[4], double* gacc_, C* psi, C* lam,
+  __device__ __forceinline__ BwdPass(const PassParams& P_, S* smem, C (*mats_)[4], real* gacc_, C* psi, C* lam,
                                      const real* params, int n_params_, double* grad_acc_, int64_t circ0,
                                      bool norm = true)
       : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_) {
@@ -1252,7 +1252,7 @@ struct BwdPass {
   __device__ __forceinline__ void grad(int g, real part) {
 #pragma unroll
     for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-    if ((tid & 31) == 0) gacc[(tid >> 5) * kMaxPassGates + g] = (double)part;
+    if ((tid & 31) == 0) gacc[(tid >> 5) * kMaxPassGates + g] = part;
   }
 
   // Eight gates at once: a transposed butterfly leaves the warp sum of value
@@ -1289,7 +1289,7 @@ struct BwdPass {
 #pragma unroll
       for (int j = 1; j < 8; ++j)
         if (which == j) g = gs[j];
-      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = (double)v[0];
+      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = v[0];
     }
   }
 
@@ -1313,7 +1313,7 @@ struct BwdPass {
         const int32_t slot = P.gate[g].slot;
         if (slot < 0) continue;
         double sum = 0.0;
-        for (int w = 0; w < nw; ++w) sum += gacc[w * kMaxPassGates + g];
+        for (int w = 0; w < nw; ++w) sum += (double)gacc[w * kMaxPassGates + g];
         atomicAdd(&grad_acc[circ * n_params + slot], sum * (double)P.gate[g].coef);
       }
     }
@@ -1333,7 +1333,7 @@ struct BwdPass {
 #define TEDQ_BWD_PROLOGUE_GENERIC(REAL, RB)                                                          \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                              \
+  __shared__ REAL tedq_gacc[8 * tedq::kMaxPassGates];                                                \
   tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  tedq_gacc, psi, lam, params, n_params, grad_acc, circ0, false);
 
@@ -1346,6 +1346,6 @@ struct BwdPass {
 #define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                  \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
   __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  __shared__ double tedq_gacc[8 * tedq::kMaxPassGates];                                                  \
+  __shared__ REAL tedq_gacc[8 * tedq::kMaxPassGates];                                                    \
   tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
                                  tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);

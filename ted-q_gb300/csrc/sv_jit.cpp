@@ -7,6 +7,7 @@
 #include <nvrtc.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 #include <sys/stat.h>
@@ -73,11 +74,19 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
   const char* real = real_of(P);
   char buf[512];
   // as many CTAs per SM as their shared memory (tile + matrices + gradient
-  // slots) allows while every thread may keep 128 registers
+  // slots) allows while every thread may keep 128 registers;
+  // TEDQ_GB300_CTAS=<f><b> (digits, e.g. 23) asks for f forward and b adjoint
+  // CTAs per SM instead (fewer registers per thread): a tuning knob for
+  // measurements
   const int threads = 1 << (P.m - P.R);
   const int tile_bytes = (adjoint ? 32 : 16) << (P.m - P.e);
-  const int static_bytes = adjoint ? 5 * 1024 + (threads / 32) * kMaxPassGates * 8 : 5 * 1024;
-  int min_blocks = std::min((227 * 1024) / (tile_bytes + static_bytes), 65536 / (threads * 128));
+  const int rsize = P.e == 1 ? 4 : 8;
+  const int static_bytes = adjoint ? 5 * 1024 + (threads / 32) * kMaxPassGates * rsize : 5 * 1024;
+  const int by_smem = (227 * 1024) / (tile_bytes + static_bytes + 1024);
+  int min_blocks = std::min(by_smem, 65536 / (threads * 128));
+  if (const char* env = getenv("TEDQ_GB300_CTAS"))
+    if (strlen(env) == 2 && env[adjoint ? 1 : 0] >= '1' && env[adjoint ? 1 : 0] <= '8')
+      min_blocks = std::min(by_smem, env[adjoint ? 1 : 0] - '0');
   min_blocks = std::max(1, std::min(min_blocks, 8));
   if (!adjoint) {
     snprintf(buf, sizeof buf,
