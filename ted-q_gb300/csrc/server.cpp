@@ -1,9 +1,10 @@
 // server.cpp -- continuous-batching server for circuit evaluations
 // (tedq_server_* in include/tedq_gb300.h).
 //
-// One worker thread per server owns a device-memory arena (the admission
-// budget, allocated once), a pinned host staging arena and a set of streams.
-// Each turn it (1) retires batches whose completion event has fired, copying
+// A server owns a device-memory arena (the admission budget, allocated
+// once), a pinned host staging arena and a set of streams, served by one
+// worker thread per size-class lane.  Each turn a worker (1) retires its
+// lane's batches whose completion event has fired, copying
 // results to their requests and returning the memory; (2) forms new batches
 // from the queue: the oldest queued request selects the program, queued
 // requests of that program (same gradient flag) join it up to max_batch, the
@@ -20,7 +21,9 @@
 // ahead of the large lane's as SMs free up), its own share of the memory
 // budget (the small lane's region is reserved, large batches cannot take it)
 // and forms batches from its own queue in arrival order.  A large circuit
-// therefore never holds a stream or memory a small one is waiting for.
+// therefore never holds a stream or memory a small one is waiting for, and
+// the small lane's worker never waits while the large lane's launches a
+// batch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -148,7 +151,7 @@ struct tedq_server {
   std::deque<std::shared_ptr<Request>> queue[2];
   std::unordered_map<int64_t, std::shared_ptr<Request>> all;
   std::vector<Batch> inflight;
-  std::thread worker;
+  std::thread workers[2];
   bool stop = false;
   bool paused = false;
   int64_t next_ticket = 1;
@@ -199,7 +202,7 @@ Layout layout(const ProgInfo& in, tedq_program_t* prog, int64_t B, bool grad) {
 
 void CUDART_CB on_batch_done(void* user) {
   auto* S = static_cast<tedq_server*>(user);
-  S->cv_work.notify_one();
+  S->cv_work.notify_all();
 }
 
 // Packs the batch's inputs, launches its work on its stream and records the
@@ -312,10 +315,14 @@ bool form_batch(tedq_server* S, Batch& b, Clock::time_point now, int lane) {
 }
 
 // Retires finished batches (lock held); returns true if any finished.
-bool retire(tedq_server* S) {
+bool retire(tedq_server* S, int lane) {
   bool any = false;
   for (size_t i = 0; i < S->inflight.size();) {
     Batch& b = S->inflight[i];
+    if (b.lane != lane) {
+      ++i;
+      continue;
+    }
     const cudaError_t q = cudaEventQuery(b.done);
     if (q == cudaErrorNotReady) {
       ++i;
@@ -362,19 +369,24 @@ void fail_queued(tedq_server* S, int32_t status) {
   S->cv_done.notify_all();
 }
 
-void worker_main(tedq_server* S) {
+// The worker of one lane: retires the lane's finished batches and launches
+// new ones on the lane's free streams (the lock is released while a batch is
+// packed and launched).
+void worker_main(tedq_server* S, int lane) {
   cudaSetDevice(S->opt.device);
   std::unique_lock<std::mutex> lk(S->mu);
   for (;;) {
+    bool mine = false;
+    for (const Batch& f : S->inflight) mine |= f.lane == lane;
     if (S->stop) {
       fail_queued(S, TEDQ_ERR_STATE);
-      if (S->inflight.empty()) break;
+      if (!mine) break;
     }
-    bool progress = retire(S);
+    bool progress = retire(S, lane);
     if (progress) S->cv_done.notify_all();
     if (!S->paused && !S->stop) {
       for (size_t si = 0; si < S->streams.size(); ++si) {
-        if (S->stream_busy[si]) continue;
+        if (S->stream_busy[si] || S->stream_lane[si] != lane) continue;
         Batch b;
         b.stream = (int)si;
         b.done = nullptr;
@@ -388,7 +400,7 @@ void worker_main(tedq_server* S) {
         progress = true;
       }
     }
-    if (!progress) S->cv_work.wait_for(lk, std::chrono::microseconds(S->inflight.empty() ? 2000 : 50));
+    if (!progress) S->cv_work.wait_for(lk, std::chrono::microseconds(mine ? 50 : 2000));
   }
 }
 
@@ -458,7 +470,7 @@ int32_t tedq_server_create(const tedq_server_options_t* opts, tedq_server_t** ou
   }
   cudaSetDevice(prev);
   tedq_server* raw = S.release();
-  raw->worker = std::thread(worker_main, raw);
+  for (int l = 2 - raw->n_lanes; l < 2; ++l) raw->workers[l] = std::thread(worker_main, raw, l);
   *out = raw;
   return TEDQ_OK;
 }
@@ -470,7 +482,8 @@ int32_t tedq_server_destroy(tedq_server_t* S) {
     S->stop = true;
   }
   S->cv_work.notify_all();
-  if (S->worker.joinable()) S->worker.join();
+  for (auto& w : S->workers)
+    if (w.joinable()) w.join();
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(S->opt.device);
@@ -505,7 +518,7 @@ int32_t tedq_server_submit(tedq_server_t* S, tedq_program_t* prog, const void* p
     S->stats.submitted++;
     *ticket = r->ticket;
   }
-  S->cv_work.notify_one();
+  S->cv_work.notify_all();
   return TEDQ_OK;
 }
 
