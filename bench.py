@@ -28,8 +28,13 @@ import sys
 import tempfile
 import time
 
-import numpy as np
-import torch
+# more hardware work queues than the driver's default 8 (before CUDA starts):
+# the serving workload's prioritised streams must not share a queue with the
+# large circuits' streams
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 for _p in (ROOT, os.path.join(ROOT, "ted-q_gb300")):

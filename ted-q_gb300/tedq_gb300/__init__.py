@@ -7,7 +7,16 @@ circuits written for TeD-Q run unchanged with ``import tedq_gb300 as qai`` and
 same backend string to an installed reference ``tedq``.
 """
 
-from .circuit import Circuit, generate_parameters  # noqa: F401
+import os as _os
+
+# Hardware work queues per CUDA context (read when the context is created,
+# i.e. effective when this package is imported before the first CUDA call).
+# The driver's default of 8 makes streams share queues, and a kernel then
+# waits in order behind another stream's kernels: the serving loop's
+# high-priority small-circuit streams would queue behind large circuits.
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+from .circuit import Circuit, generate_parameters  # noqa: F401,E402
 from .errors import BackendError, QuantumCircuitError, QuantumStorageError, QuantumValueError  # noqa: F401
 from .measurement import (Expectation, MeasurementReturnTypes, Probability, QuantumMeasurement,  # noqa: F401
                           State, expval, probs, sample, state, var)

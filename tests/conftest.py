@@ -4,6 +4,9 @@ import sys
 
 import pytest
 
+# hardware work queues: set before CUDA starts, as the package does on import
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG_ROOT = os.path.join(ROOT, "ted-q_gb300")
 for p in (ROOT, PKG_ROOT):
