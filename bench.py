@@ -530,8 +530,9 @@ def cpu_service_model(sizes, depths, budget_s):
     oracle's per-gate tensordot loop, value + gradient by back_prop,
     complex64, all host threads) for every (n, depth) of the serving stream.
     n <= 16: measured at the smallest, middle and largest depth, linear in
-    depth between; n = 20, 24: measured at the smallest depth and scaled
-    linearly in depth (the loop's cost is proportional to the gate count).
+    depth between; n = 20: measured at the smallest depth and scaled linearly
+    in depth (the loop's cost is proportional to the gate count); n = 24:
+    the n = 20 time scaled by the state size (16x) and the gate count.
     Returns ({(n, d): seconds}, description)."""
     import oracle
     from tedq_gb300.templates import hea_spec
@@ -548,20 +549,27 @@ def cpu_service_model(sizes, depths, budget_s):
     d0, d1, d2 = depths[0], depths[len(depths) // 2], depths[-1]
     model, t_start = {}, time.perf_counter()
     one(4, d0)  # warm-up
+    n_gates = lambda n, d: len(hea_spec(n, d)["gates"])  # noqa: E731
+    t20 = None
     for n in sizes:
         if n <= 16:
             pts = {d: one(n, d) for d in (d0, d1, d2)}
             for d in depths:
                 lo, hi = (d0, d1) if d <= d1 else (d1, d2)
                 model[(n, d)] = pts[lo] + (pts[hi] - pts[lo]) * (d - lo) / (hi - lo)
-        else:
-            t = one(n, d0)
+        elif n == 20:
+            t20 = one(n, d0)
             for d in depths:
-                model[(n, d)] = t * d / d0
+                model[(n, d)] = t20 * d / d0
+    for n in sizes:
+        if n > 20:
+            for d in depths:
+                model[(n, d)] = t20 * (2.0 ** (n - 20)) * n_gates(n, d) / n_gates(20, d0)
     desc = (f"reference algorithm per request on the host (oracle port, back_prop, complex64, "
             f"{torch.get_num_threads()} threads): n <= 16 measured at depths {d0}, {d1}, {d2} and interpolated, "
-            f"n > 16 measured at depth {d0} and scaled by depth; {time.perf_counter() - t_start:.1f} s of "
-            f"measurement; the identical trace replayed through a sequential FIFO server with these times")
+            f"n = 20 measured at depth {d0} and scaled by depth, n = 24 extrapolated from n = 20 by state size and "
+            f"gate count; {time.perf_counter() - t_start:.1f} s of measurement; the identical trace replayed "
+            f"through a sequential FIFO server with these times")
     return model, desc
 
 
