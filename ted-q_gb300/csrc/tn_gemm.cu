@@ -168,6 +168,23 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+// 16 / 32 consecutive accumulator columns of this thread's lane in one
+// instruction (no wait: the caller waits once for all its loads)
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // 8 consecutive accumulator columns of this thread's lane
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
@@ -444,12 +461,22 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
       if (!ok) return;
       tc_fence_after();
       const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN + half * HALF);
+      if constexpr (HALF % 16 == 0) {
+        // every load of the group in flight together, one wait
+        float v[HALF];
 #pragma unroll
-      for (int c0 = 0; c0 < HALF; c0 += 8) {
-        float v[8];
-        tmem_ld8(base + (uint32_t)c0, v);
+        for (int c0 = 0; c0 < HALF; c0 += 16) tmem_ld16_nowait(base + (uint32_t)c0, v + c0);
+        tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[c0 + j] += v[j];
+        for (int j = 0; j < HALF; ++j) acc[j] += v[j];
+      } else {
+#pragma unroll
+        for (int c0 = 0; c0 < HALF; c0 += 8) {
+          float v[8];
+          tmem_ld8(base + (uint32_t)c0, v);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[c0 + j] += v[j];
+        }
       }
       tc_fence_before();
       __syncwarp();
