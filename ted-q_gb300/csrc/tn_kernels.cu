@@ -104,9 +104,8 @@ __global__ void __launch_bounds__(256) tn_leaf_kernel(const TnLeafDesc* __restri
 // one word per 32) and written out in destination order, so both sides are
 // coalesced.  Tile-local offsets are tabulated once per CTA in the order each
 // phase uses them (32-bit: the host limits operands to 2^28 entries), the
-// low 8 outer element bits likewise; every CTA keeps the loads of two tiles
-// in flight (the tile after next is loaded while the current one is written
-// out).
+// low 8 outer element bits likewise; the next tile's loads are issued before
+// the current tile is written out.
 template <typename real>
 __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ TnGatherArgs A) {
   constexpr int TS_MAX = 1 << kTnTileBits, PER = TS_MAX / 256;
@@ -164,12 +163,11 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
   const real* __restrict__ src = static_cast<const real*>(A.op[op].src);
   real* __restrict__ dst = static_cast<real*>(A.op[op].dst);
   const int lomask = (1 << nlo) - 1;
-  // two tiles' loads in flight per CTA: register sets a and b alternate
-  real ar[PER], ai[PER], br[PER], bi[PER];
-  int64_t tile = blockIdx.x, da = 0, db = 0;
+  real vr[PER], vi[PER];
+  int64_t tile = blockIdx.x, dcur = 0;
   using V2 = typename std::conditional<sizeof(real) == 4, float2, double2>::type;
   const int rmode = A.op[op].rmode, wpair = A.op[op].wpair;
-  auto load = [&](int64_t t, real (&vr)[PER], real (&vi)[PER]) {
+  auto load = [&](int64_t t) {
     const int64_t b = t >> outer, ou = t & ((1ll << outer) - 1);
     int64_t so = src_base + b * src_bstride + olo_s[ou & lomask];
     int64_t dof = b * dstride + olo_d[ou & lomask];
@@ -216,10 +214,8 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
     }
     return dof;
   };
-  // tile t from the registers (vr, vi) loaded for it; the registers then
-  // take the loads of tile t + 2 * grid while tile t is written out
-  auto step = [&](int64_t t, real (&vr)[PER], real (&vi)[PER], int64_t& dcur) {
-    if (t >= total) return;
+  if (tile < total) dcur = load(tile);
+  for (; tile < total; tile += gridDim.x) {
     if (rmode == 1) {
 #pragma unroll
       for (int q = 0; q < PER / 2; ++q) {
@@ -245,7 +241,7 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
     }
     __syncthreads();
     real* d = dst + dcur;
-    if (t + 2 * (int64_t)gridDim.x < total) dcur = load(t + 2 * (int64_t)gridDim.x, vr, vi);
+    if (tile + gridDim.x < total) dcur = load(tile + gridDim.x);
     if (wpair) {
 #pragma unroll
       for (int q = 0; q < PER / 2; ++q) {
@@ -283,12 +279,6 @@ __global__ void __launch_bounds__(256) tn_gather_kernel(const __grid_constant__ 
       }
     }
     __syncthreads();
-  };
-  if (tile < total) da = load(tile, ar, ai);
-  if (tile + gridDim.x < total) db = load(tile + gridDim.x, br, bi);
-  for (; tile < total; tile += 2 * (int64_t)gridDim.x) {
-    step(tile, ar, ai, da);
-    step(tile + gridDim.x, br, bi, db);
   }
 }
 
