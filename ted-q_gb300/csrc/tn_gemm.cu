@@ -16,7 +16,7 @@
 // FP32 registers with round-to-nearest, which keeps the result at FP32
 // accuracy for long K.  One CTA computes a 128-row
 // tile of the larger side (the "P" operand) against a BN-column tile of the
-// other ("Q"), BN in {16, 32, 64, 128}; persistent CTAs (one per SM) walk
+// other ("Q"), BN in {16, 32, 64, 128, 256}; persistent CTAs (one per SM) walk
 // their tiles with the pipeline running on across tile boundaries; warps:
 //   warp 0     TMA producer: 3-D tensor maps [batch][rows][k], 128-byte
 //              swizzle, boxes of 32 K-elements (one swizzle row);
@@ -462,13 +462,17 @@ __global__ void __launch_bounds__(TcWarps<BN>::kThreads, 1)
       tc_fence_after();
       const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN + half * HALF);
       if constexpr (HALF % 16 == 0) {
-        // every load of the group in flight together, one wait
-        float v[HALF];
+        // up to 32 columns of loads in flight together, one wait each
+        constexpr int CH = HALF < 32 ? HALF : 32;
 #pragma unroll
-        for (int c0 = 0; c0 < HALF; c0 += 16) tmem_ld16_nowait(base + (uint32_t)c0, v + c0);
-        tmem_wait_ld();
+        for (int c1 = 0; c1 < HALF; c1 += CH) {
+          float v[CH];
 #pragma unroll
-        for (int j = 0; j < HALF; ++j) acc[j] += v[j];
+          for (int c0 = 0; c0 < CH; c0 += 16) tmem_ld16_nowait(base + (uint32_t)(c1 + c0), v + c0);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < CH; ++j) acc[c1 + j] += v[j];
+        }
       } else {
 #pragma unroll
         for (int c0 = 0; c0 < HALF; c0 += 8) {
@@ -678,6 +682,8 @@ cudaError_t dispatch_kb(int kb, const CUtensorMap& mp, const CUtensorMap& mq, co
 template <bool SPLIT>
 cudaError_t dispatch_split(int bn, int kb, const CUtensorMap& mp, const CUtensorMap& mq, const TcWork& w, int* err,
                            cudaStream_t s) {
+  if (bn == 256) return kb == 8 ? launch_tc<256, SPLIT, 8>(mp, mq, w, err, s)
+                                 : launch_tc<256, SPLIT, 16>(mp, mq, w, err, s);
   if (bn == 128) return dispatch_kb<128, SPLIT>(kb, mp, mq, w, err, s);
   if (bn == 64) return dispatch_kb<64, SPLIT>(kb, mp, mq, w, err, s);
   if (bn == 32) return dispatch_kb<32, SPLIT>(kb, mp, mq, w, err, s);
@@ -702,12 +708,21 @@ bool tn_gemm_tc_supported(const TnGemmArgs& g) {
 
 cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   // the larger side fills the 128-row tiles
-  const bool swap = g.nr > g.mr;
+  // Which side fills the 128-row tiles: the larger one, or, when both sides
+  // have at least 128 rows and one at least 256, the smaller one with N = 256
+  // MMAs on the other (twice the flops per operand byte of N = 128).
+  static const bool wide_ok = [] {
+    const char* e = getenv("TEDQ_GB300_TN_GEMM_N256");  // tuning knob: 0 turns N = 256 off
+    return !(e && e[0] == '0');
+  }();
+  const int64_t lo_side = g.mr < g.nr ? g.mr : g.nr, hi_side = g.mr < g.nr ? g.nr : g.mr;
+  const bool wide = wide_ok && lo_side >= 128 && hi_side >= 256;
+  const bool swap = wide ? g.nr < g.mr : g.nr > g.mr;
   const float* P = static_cast<const float*>(swap ? g.b : g.a);
   const float* Q = static_cast<const float*>(swap ? g.a : g.b);
   const int64_t pe = swap ? g.nr : g.mr, qe = swap ? g.mr : g.nr;
   const int64_t sp = swap ? g.sb : g.sa, sq = swap ? g.sa : g.sb;
-  const int bn = qe >= 128 ? 128 : qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
+  const int bn = wide ? 256 : qe >= 128 ? 128 : qe >= 64 ? 64 : qe >= 32 ? 32 : 16;
   // K per stage: one swizzle row of 32 values, or 16 / 8 for short sums (no
   // zero-filled MMAs)
   // TEDQ_GB300_TN_GEMM_KB (8, 16 or 32) caps it: a tuning knob for measurements
@@ -718,6 +733,7 @@ cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   }();
   int kb = g.kr <= 8 ? 8 : g.kr <= 16 ? 16 : 32;
   kb = kb < kb_cap ? kb : kb_cap;
+  if (bn == 256 && kb > 16) kb = 16;  // shared memory: the N = 256 operand slots
   CUtensorMap mp, mq;
   if (!make_map(&mp, P, pe, g.kr, g.nbatch, sp, 128, kb) || !make_map(&mq, Q, qe, g.kr, g.nbatch, sq, bn, kb))
     return cudaErrorInvalidValue;
