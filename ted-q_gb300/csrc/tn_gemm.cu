@@ -708,12 +708,14 @@ bool tn_gemm_tc_supported(const TnGemmArgs& g) {
 
 cudaError_t tn_gemm_tc(const TnGemmArgs& g, bool split, cudaStream_t s) {
   // the larger side fills the 128-row tiles
-  // Which side fills the 128-row tiles: the larger one, or, when both sides
-  // have at least 128 rows and one at least 256, the smaller one with N = 256
-  // MMAs on the other (twice the flops per operand byte of N = 128).
+  // Which side fills the 128-row tiles: the larger one.  Tuning knob
+  // TEDQ_GB300_TN_GEMM_N256=1: when both sides have at least 128 rows and one
+  // at least 256, the smaller one with N = 256 MMAs on the other (twice the
+  // flops per operand byte; measured slower: 64 accumulators per thread spill
+  // and the operand slots leave room for K-blocks of 16 only).
   static const bool wide_ok = [] {
-    const char* e = getenv("TEDQ_GB300_TN_GEMM_N256");  // tuning knob: 0 turns N = 256 off
-    return !(e && e[0] == '0');
+    const char* e = getenv("TEDQ_GB300_TN_GEMM_N256");
+    return e && e[0] == '1';
   }();
   const int64_t lo_side = g.mr < g.nr ? g.mr : g.nr, hi_side = g.mr < g.nr ? g.nr : g.mr;
   const bool wide = wide_ok && lo_side >= 128 && hi_side >= 256;
