@@ -3,9 +3,12 @@
 // sv_jit.cpp generates and compiles with NVRTC at program-creation time.
 //
 // A pass kernel is written as
-//     FwdPass<real, R> c(...);          // matrices + tile staging
-//     c.begin(f); <gates on c.a>; c.end(f);   // one register phase
-//     c.finish();                       // tile back to HBM
+//     FwdPass<real, R> c(...);          // slots, first tile fetches
+//     while (c.next()) {                // next tile of this thread group
+//       c.begin(f); <gates on c.a>; c.end(f);   // one register phase
+//       c.finish();                     // tile back to HBM, slot refilled
+//     }
+//     c.close();
 // In the generic kernels the gates of a phase are dispatched at run time; in
 // the generated kernels every gate is a template instance with its register
 // bit and control mask as compile-time constants, so control tests fold away
@@ -178,6 +181,42 @@ __device__ __forceinline__ SUnit<double> regs_st(const Regs<double, R>& A, int j
   s.v = A.a[j];
   return s;
 }
+
+// The same for a unit still in HBM order (complex64: re0, im0, re1, im1): the
+// tile as the asynchronous copies leave it and as it goes back to HBM.
+template <int R>
+__device__ __forceinline__ void regs_ld_raw(Regs<float, R>& A, int j, const SUnit<float>& s) {
+  A.re[j] = make_float2(s.re.x, s.im.x);
+  A.im[j] = make_float2(s.re.y, s.im.y);
+}
+template <int R>
+__device__ __forceinline__ SUnit<float> regs_st_raw(const Regs<float, R>& A, int j) {
+  SUnit<float> s;
+  s.re = make_float2(A.re[j].x, A.im[j].x);
+  s.im = make_float2(A.re[j].y, A.im[j].y);
+  return s;
+}
+template <int R>
+__device__ __forceinline__ void regs_ld_raw(Regs<double, R>& A, int j, const SUnit<double>& s) {
+  A.a[j] = s.v;
+}
+template <int R>
+__device__ __forceinline__ SUnit<double> regs_st_raw(const Regs<double, R>& A, int j) {
+  SUnit<double> s;
+  s.v = A.a[j];
+  return s;
+}
+
+// HBM order <-> pair-planar order of one shared-memory unit.
+__device__ __forceinline__ SUnit<float> raw_to_s(const SUnit<float>& r) {
+  SUnit<float> s;
+  s.re = make_float2(r.re.x, r.im.x);
+  s.im = make_float2(r.re.y, r.im.y);
+  return s;
+}
+__device__ __forceinline__ SUnit<double> raw_to_s(const SUnit<double>& r) { return r; }
+__device__ __forceinline__ SUnit<float> s_to_raw(const SUnit<float>& s) { return raw_to_s(s); }
+__device__ __forceinline__ SUnit<double> s_to_raw(const SUnit<double>& s) { return s; }
 
 // packed FP32x2 helpers
 __device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
@@ -890,35 +929,41 @@ __device__ __forceinline__ float grad_part(const Regs<float, R>& p, const Regs<f
     if (G == GR_P1) acc += ap.y - an.y;
     return acc;
   } else {
+    // two accumulator pairs alternate between group pairs: half-length chains
+    float2 bp = make_float2(0.f, 0.f), bn = make_float2(0.f, 0.f);
+    int par = 0;
 #pragma unroll
     for (int g = 0; g < NG; ++g) {
       if (g & (1 << (K - 1))) continue;
       if ((g & cg) != cg) continue;
       const int h = g | (1 << (K - 1));
+      float2& xp = par ? bp : ap;
+      float2& xn = par ? bn : an;
+      par ^= 1;
       if (G == GR_X) {
-        ap = fma2(l.re[g], p.im[h], ap);
-        an = fma2(l.im[g], p.re[h], an);
-        ap = fma2(l.re[h], p.im[g], ap);
-        an = fma2(l.im[h], p.re[g], an);
+        xp = fma2(l.re[g], p.im[h], xp);
+        xn = fma2(l.im[g], p.re[h], xn);
+        xp = fma2(l.re[h], p.im[g], xp);
+        xn = fma2(l.im[h], p.re[g], xn);
       }
       if (G == GR_Y) {
-        ap = fma2(l.re[h], p.re[g], ap);
-        ap = fma2(l.im[h], p.im[g], ap);
-        an = fma2(l.re[g], p.re[h], an);
-        an = fma2(l.im[g], p.im[h], an);
+        xp = fma2(l.re[h], p.re[g], xp);
+        xp = fma2(l.im[h], p.im[g], xp);
+        xn = fma2(l.re[g], p.re[h], xn);
+        xn = fma2(l.im[g], p.im[h], xn);
       }
       if (G == GR_Z) {
-        ap = fma2(l.re[g], p.im[g], ap);
-        an = fma2(l.im[g], p.re[g], an);
-        an = fma2(l.re[h], p.im[h], an);
-        ap = fma2(l.im[h], p.re[h], ap);
+        xp = fma2(l.re[g], p.im[g], xp);
+        xn = fma2(l.im[g], p.re[g], xn);
+        xn = fma2(l.re[h], p.im[h], xn);
+        xp = fma2(l.im[h], p.re[h], xp);
       }
       if (G == GR_P1) {
-        ap = fma2(l.re[h], p.im[h], ap);
-        an = fma2(l.im[h], p.re[h], an);
+        xp = fma2(l.re[h], p.im[h], xp);
+        xn = fma2(l.im[h], p.re[h], xn);
       }
     }
-    const float dx = ap.x - an.x, dy = ap.y - an.y;
+    const float dx = (ap.x - an.x) + (bp.x - bn.x), dy = (ap.y - an.y) + (bp.y - bn.y);
     return c0 ? dy : dx + dy;
   }
 }
@@ -1071,10 +1116,81 @@ __device__ __forceinline__ void thread_offsets(const PassParams& P, int tid, int
     }
 }
 
-// ---------------------------------------------------------------- forward pass
+// ---------------------------------------------------------------- tile pipeline
+// A pass kernel is persistent: CTA b takes a contiguous range of the launch's
+// tiles (tile index = circuit * 2^(n-m) + tile of the circuit) and runs it in
+// G thread groups that take the range's tiles in turn (group k % G takes tile
+// k).  Tile k lives in slot k % (G + 1).  When a group has written tile k
+// back to HBM it issues the asynchronous copies (cp.async, 16 bytes a thread)
+// of tile k + G + 1 into the slot it just freed, so HBM reads run while the
+// groups compute; the copies arrive on the slot's mbarrier, which the group
+// owning the tile waits on.  Groups synchronise with their own named barrier
+// and never wait on each other except through the slot mbarriers, so one
+// group's shared-memory transitions overlap the other's arithmetic.  The
+// matrices are built once per circuit and group, adjoint gradients are summed
+// per warp in FP64 over all tiles of a circuit and added to HBM once.
 
-template <typename real, int R>
-struct FwdPass {
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* b, unsigned parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Waits for the completion of the mbarrier phase of the given parity; gives
+// up after about half a second (2^21 polls, sleeping between the later ones)
+// and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+  for (uint32_t i = 0; i < (1u << 21); ++i) {
+    if (mbar_test(b, parity)) return true;
+    if (i >= 32) __nanosleep(i < 1024 ? 32 : 256);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(b)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// The mbarrier counts one arrival of this thread once all its earlier
+// cp.async copies have landed.
+__device__ __forceinline__ void cp_async_arrive(uint64_t* b) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+template <typename real>
+__device__ __forceinline__ Unit<real> nan_unit() {
+  Unit<real> v;
+  const real q = (real)__int_as_float(0x7fc00000);
+#pragma unroll
+  for (int k = 0; k < (1 << UnitsPerAmp<real>::E); ++k) v.v[k] = mk<real>(q, q);
+  return v;
+}
+
+// Tile bookkeeping shared by the forward and the adjoint pass.
+template <typename real, int R, bool ADJ>
+struct Pipe {
   using C = cpx<real>;
   using U = Unit<real>;
   using S = SUnit<real>;
@@ -1082,74 +1198,234 @@ struct FwdPass {
   static constexpr int NR = 1 << R;
   static constexpr int NU = NR >> E;
   const PassParams& P;
-  S* tile;
+  S* slots;
+  uint32_t su;     // units per slot
+  uint32_t half;   // adjoint: offset of lambda inside a slot (units)
+  S* tile;         // slot of the current tile
+  C (*mats)[4];    // this group's matrices
+  uint64_t* mbar;  // one per slot
+  C* psi;
+  C* lam;
+  const real* params;
+  int n_params;
+  int G, g, T, tid, bar;
+  int64_t t0, cnt, k, circ;
+  uint64_t gth;    // thread part of the global staging offsets
+  uint32_t sthr;   // thread part of the shared-memory staging units
+  uint64_t gthr;   // current tile: global offset base of this thread
+  C* st;           // current circuit's psi
+  C* sl;           // current circuit's lambda
+  bool ok;         // false once a slot wait gave up (outputs become NaN)
+  bool norm;
+
+  __device__ __forceinline__ Pipe(const PassParams& P_, unsigned char* smem, C* psi_, C* lam_, const real* params_,
+                                  int n_params_, int64_t n_tiles, bool norm_)
+      : P(P_), psi(psi_), lam(lam_), params(params_), n_params(n_params_), norm(norm_) {
+    T = 1 << (P.m - R);
+    G = (int)blockDim.x / T;
+    g = (int)threadIdx.x / T;
+    tid = (int)threadIdx.x - g * T;
+    bar = 1 + g;
+    const PipeLayout L = pipe_layout(P, G, ADJ);
+    slots = reinterpret_cast<S*>(smem);
+    su = L.slot_bytes >> 4;
+    half = su >> 1;
+    const int nm = P.n_mats > 0 ? P.n_mats : 1;
+    mats = reinterpret_cast<C(*)[4]>(smem + L.mats_off) + g * nm;
+    mbar = reinterpret_cast<uint64_t*>(smem + L.mbar_off);
+    const int64_t per = n_tiles / gridDim.x, rem = n_tiles % gridDim.x, b = blockIdx.x;
+    t0 = b * per + (b < rem ? b : rem);
+    cnt = per + (b < rem ? 1 : 0);
+    gth = 0;
+    sthr = 0;
+    thread_offsets(P, tid, P.m - R, gth, sthr);
+    if (threadIdx.x == 0)
+      for (int s = 0; s <= G; ++s) mbar_init(&mbar[s], (unsigned)T);
+    k = g - G;
+    circ = -1;
+    ok = true;
+    tile = slots;
+    st = sl = nullptr;
+    gthr = 0;
+  }
+
+  // First tiles: tile j < G + 1 is fetched by group (j + G - 1) % G, the group
+  // that fetches every later tile of its slot.  Call after the CTA barrier
+  // that publishes the mbarrier initialisation.
+  __device__ __forceinline__ void start(const C* init) {
+    for (int j = 0; j <= G && j < cnt; ++j)
+      if ((j + G - 1) % G == g) fetch(j, init);
+  }
+
+  __device__ __forceinline__ void fetch(int64_t kk, const C* init) {
+    const int s = (int)(kk % (G + 1));
+    S* dst = slots + (size_t)s * su;
+    const int64_t gt = t0 + kk;
+    const int64_t c = gt >> (P.n - P.m);
+    const uint32_t tic = (uint32_t)(gt & ((1ll << (P.n - P.m)) - 1));
+    const uint64_t gb = tile_base(P, tic) | gth;
+    const C* src = psi + (c << P.n);
+    if (ADJ || P.init == 0) {
+#pragma unroll
+      for (int q = 0; q < NU; ++q) cp_async16(dst + (sthr ^ P.sk[q]), reinterpret_cast<const U*>(src) + ((gb | P.gk[q]) >> E));
+      if (ADJ) {
+        const C* srl = lam + (c << P.n);
+#pragma unroll
+        for (int q = 0; q < NU; ++q)
+          cp_async16(dst + half + (sthr ^ P.sk[q]), reinterpret_cast<const U*>(srl) + ((gb | P.gk[q]) >> E));
+      }
+      cp_async_arrive(&mbar[s]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < NU; ++q)
+        *reinterpret_cast<U*>(dst + (sthr ^ P.sk[q])) = load_unit<real>(P, src, gb | P.gk[q], init);
+      mbar_arrive(&mbar[s]);
+    }
+  }
+
+  // Next tile of this group: waits for its slot; on a new circuit the caller
+  // rebuilds the matrices (returns 2), else returns 1; 0 = no tile left.
+  __device__ __forceinline__ int advance() {
+    k += G;
+    if (k >= cnt) return 0;
+    const int s = (int)(k % (G + 1));
+    if (ok && !mbar_wait(&mbar[s], (unsigned)((k / (G + 1)) & 1))) ok = false;
+    tile = slots + (size_t)s * su;
+    const int64_t gt = t0 + k;
+    const int64_t c = gt >> (P.n - P.m);
+    gthr = tile_base(P, (uint32_t)(gt & ((1ll << (P.n - P.m)) - 1))) | gth;
+    if (c == circ) return 1;
+    circ = c;
+    st = psi + (c << P.n);
+    if (ADJ) sl = lam + (c << P.n);
+    return 2;
+  }
+
+  // Matrices of the current circuit (the previous tile's last group barrier
+  // guarantees no thread of the group still reads the old ones).
+  __device__ __forceinline__ void build_mats() {
+    const real* prm = params ? params + circ * n_params : nullptr;
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
+    group_sync(bar, T);
+    if (norm && P.norm_last != kNoNorm) {
+      norm_scan<real>(P, mats, tid);
+      group_sync(bar, T);
+    }
+  }
+
+  // Converts the current tile between HBM order and pair-planar order (needed
+  // around a dense phase that opens or closes a pass), then syncs the group.
+  __device__ __forceinline__ void convert(bool to_planar) {
+    for (uint32_t u = (uint32_t)tid; u < su; u += (uint32_t)T) tile[u] = to_planar ? raw_to_s(tile[u]) : s_to_raw(tile[u]);
+    group_sync(bar, T);
+  }
+
+  // Writes the current tile back and refills its slot with tile k + G + 1.
+  __device__ __forceinline__ void write_back(const C* init) {
+    U* gp = reinterpret_cast<U*>(st);
+#pragma unroll
+    for (int q = 0; q < NU; ++q) {
+      U v = *reinterpret_cast<const U*>(tile + (sthr ^ P.sk[q]));
+      if (!ok) v = nan_unit<real>();
+      gp[(gthr | P.gk[q]) >> E] = v;
+    }
+    if (ADJ) {
+      U* gl = reinterpret_cast<U*>(sl);
+#pragma unroll
+      for (int q = 0; q < NU; ++q) {
+        U v = *reinterpret_cast<const U*>(tile + half + (sthr ^ P.sk[q]));
+        if (!ok) v = nan_unit<real>();
+        gl[(gthr | P.gk[q]) >> E] = v;
+      }
+    }
+    group_sync(bar, T);
+    const int64_t kk = k + G + 1;
+    if (kk < cnt) fetch(kk, init);
+  }
+};
+
+// ---------------------------------------------------------------- forward pass
+
+template <typename real, int R>
+struct FwdPass {
+  using C = cpx<real>;
+  using S = SUnit<real>;
+  static constexpr int E = UnitsPerAmp<real>::E;
+  static constexpr int NR = 1 << R;
+  static constexpr int NU = NR >> E;
+  Pipe<real, R, false> p;
+  const C* init;
   C (*mats)[4];
-  C* st;
-  int tid;
-  uint64_t gthr;
-  uint32_t sthr;
   uint32_t bu;
   Regs<real, R> a;
 
-  __device__ __forceinline__ FwdPass(const PassParams& P_, S* tile_, C (*mats_)[4], C* psi, const real* params,
-                                     int n_params, const C* init, int64_t circ0, bool norm = true)
-      : P(P_), tile(tile_), mats(mats_) {
-    tid = threadIdx.x;
-    const int T = blockDim.x;
-    const int64_t circ = circ0 + blockIdx.y;
-    st = psi + (circ << P.n);
-    const real* prm = params ? params + circ * n_params : nullptr;
-    gthr = tile_base(P, blockIdx.x);
-    sthr = 0;
-    thread_offsets(P, tid, P.m - R, gthr, sthr);
-    U v[NU];
-#pragma unroll
-    for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
-    // matrices while the tile loads are in flight
-    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
-    if (norm && P.norm_last != kNoNorm) {
-      __syncthreads();
-      norm_scan<real>(P, mats, tid);
-    }
-#pragma unroll
-    for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = to_s(v[k]);
+  __device__ __forceinline__ FwdPass(const PassParams& P_, unsigned char* smem, C* psi, const real* params,
+                                     int n_params, const C* init_, int64_t n_tiles, bool norm = true)
+      : p(P_, smem, psi, nullptr, params, n_params, n_tiles, norm), init(init_) {
+    mats = p.mats;
     __syncthreads();
+    p.start(init);
   }
 
-  __device__ __forceinline__ void begin(int f) {
-    const Phase& ph = P.phase[f];
+  // next tile of this thread's group (false: none left)
+  __device__ __forceinline__ bool next() {
+    const int r = p.advance();
+    if (r == 2) p.build_mats();
+    return r != 0;
+  }
+
+  // Register phases read the tile in pair-planar order, except the first,
+  // which reads it as the copies left it (HBM order); the last writes it back
+  // in HBM order.
+  __device__ __forceinline__ void load(int f, bool raw) {
+    const Phase& ph = p.P.phase[f];
     bu = 0;
     for (int b = 0; b < ph.ntid; ++b)
-      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+      if ((p.tid >> b) & 1) bu ^= ph.tid_off[b];
 #pragma unroll
-    for (int j = 0; j < NU; ++j) regs_ld(a, j, tile[bu ^ ph.reg_off[j]]);
+    for (int j = 0; j < NU; ++j) {
+      if (raw) regs_ld_raw(a, j, p.tile[bu ^ ph.reg_off[j]]);
+      else regs_ld(a, j, p.tile[bu ^ ph.reg_off[j]]);
+    }
   }
 
-  __device__ __forceinline__ void end(int f) {
-    const Phase& ph = P.phase[f];
+  __device__ __forceinline__ void store(int f, bool raw) {
+    const Phase& ph = p.P.phase[f];
 #pragma unroll
-    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
-    __syncthreads();
+    for (int j = 0; j < NU; ++j) p.tile[bu ^ ph.reg_off[j]] = raw ? regs_st_raw(a, j) : regs_st(a, j);
+  }
+
+  __device__ __forceinline__ void begin(int f) { load(f, false); }
+  __device__ __forceinline__ void begin_first(int f) { load(f, true); }
+
+  __device__ __forceinline__ void end(int f) {
+    store(f, false);
+    group_sync(p.bar, p.T);
+  }
+
+  __device__ __forceinline__ void end_last(int f) {
+    store(f, true);
+    group_sync(p.bar, p.T);
   }
 
   // end of a phase whose successor is warp-local (Phase::wlocal)
   __device__ __forceinline__ void end_w(int f) {
-    const Phase& ph = P.phase[f];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
+    store(f, false);
     __syncwarp();
   }
 
+  // dense phases work in pair-planar order: to_planar() before one that opens
+  // the pass, to_raw() after one that closes it
   __device__ __forceinline__ void dense(int f) {
-    dense_phase<real>(P, P.phase[f], tile, tid, blockDim.x);
-    __syncthreads();
+    dense_phase<real>(p.P, p.P.phase[f], p.tile, p.tid, p.T);
+    group_sync(p.bar, p.T);
   }
+  __device__ __forceinline__ void to_planar() { p.convert(true); }
+  __device__ __forceinline__ void to_raw() { p.convert(false); }
 
-  __device__ __forceinline__ void finish() {
-    U* gst = reinterpret_cast<U*>(st);
-#pragma unroll
-    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = from_s(tile[sthr ^ P.sk[k]]);
-  }
+  __device__ __forceinline__ void finish() { p.write_back(init); }
+
+  __device__ __forceinline__ void close() { cp_async_wait_all(); }
 };
 
 // ---------------------------------------------------------------- adjoint pass
@@ -1157,102 +1433,139 @@ struct FwdPass {
 template <typename real, int R>
 struct BwdPass {
   using C = cpx<real>;
-  using U = Unit<real>;
   using S = SUnit<real>;
   static constexpr int E = UnitsPerAmp<real>::E;
   static constexpr int NR = 1 << R;
   static constexpr int NU = NR >> E;
-  const PassParams& P;
-  S* tp;
-  S* tl;
+  Pipe<real, R, true> p;
   C (*mats)[4];
-  real* gacc;  // per-warp gradient partials (the warp sums, in the state's precision)
-  C* sp;
-  C* sl;
+  real* gacc;     // this group's per-warp gradient partials [warp][gate] (a few tiles)
+  double* gsum;   // this group's FP64 gradient sums [gate] of the current circuit
   double* grad_acc;
-  int64_t circ;
-  int n_params;
-  int tid;
-  uint64_t gthr;
-  uint32_t sthr;
+  int ng;
+  int since_fold;  // tiles whose partials are still in gacc
   uint32_t bu;
   Regs<real, R> a;
   Regs<real, R> l;
 
-  __device__ __forceinline__ BwdPass(const PassParams& P_, S* smem, C (*mats_)[4], real* gacc_, C* psi, C* lam,
-                                     const real* params, int n_params_, double* grad_acc_, int64_t circ0,
+  // tiles a warp's partials stay in the state's precision before they are
+  // folded into the FP64 sums
+  static constexpr int kFoldTiles = 8;
+
+  __device__ __forceinline__ BwdPass(const PassParams& P_, unsigned char* smem, C* psi, C* lam,
+                                     const real* params, int n_params, double* grad_acc_, int64_t n_tiles,
                                      bool norm = true)
-      : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_) {
-    tid = threadIdx.x;
-    const int T = blockDim.x;
-    tp = smem;
-    tl = smem + (1 << (P.m - E));
-    circ = circ0 + blockIdx.y;
-    sp = psi + (circ << P.n);
-    sl = lam + (circ << P.n);
-    const real* prm = params ? params + circ * n_params : nullptr;
-    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
-    if (norm && P.norm_last != kNoNorm) {
-      __syncthreads();
-      norm_scan<real>(P, mats, tid);
-    }
-    gthr = tile_base(P, blockIdx.x);
-    sthr = 0;
-    thread_offsets(P, tid, P.m - R, gthr, sthr);
-    U v[NU], w[NU];
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      const uint64_t g = (gthr | P.gk[k]) >> E;
-      v[k] = reinterpret_cast<const U*>(sp)[g];
-      w[k] = reinterpret_cast<const U*>(sl)[g];
-    }
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      tp[sthr ^ P.sk[k]] = to_s(v[k]);
-      tl[sthr ^ P.sk[k]] = to_s(w[k]);
-    }
+      : p(P_, smem, psi, lam, params, n_params, n_tiles, norm), grad_acc(grad_acc_) {
+    mats = p.mats;
+    ng = p.P.n_gates > 0 ? p.P.n_gates : 1;
+    since_fold = 0;
+    const int W = p.T >= 32 ? p.T / 32 : 1;
+    const PipeLayout L = pipe_layout(p.P, p.G, true);
+    gsum = reinterpret_cast<double*>(smem + L.gacc_off) + (size_t)p.g * ng;
+    gacc = reinterpret_cast<real*>(smem + L.gacc_off + (size_t)p.G * ng * 8) + (size_t)p.g * W * ng;
+    for (int i = p.tid; i < W * ng; i += p.T) gacc[i] = (real)0;
+    for (int i = p.tid; i < ng; i += p.T) gsum[i] = 0.0;
     __syncthreads();
+    p.start(nullptr);
   }
 
-  __device__ __forceinline__ void begin(int f) {
-    const Phase& ph = P.phase[f];
+  // Folds the warps' partials into the FP64 sums.  Thread t owns gates
+  // t, t + T, ...; called where every warp of the group has passed a group
+  // barrier since its last partial and before the next tile's partials.
+  __device__ __forceinline__ void fold() {
+    const int W = p.T >= 32 ? p.T / 32 : 1;
+    for (int gi = p.tid; gi < p.P.n_gates; gi += p.T) {
+      double sum = 0.0;
+      for (int w = 0; w < W; ++w) {
+        sum += (double)gacc[w * ng + gi];
+        gacc[w * ng + gi] = (real)0;
+      }
+      gsum[gi] += sum;
+    }
+    since_fold = 0;
+  }
+
+  // Adds this group's gradient sums of the current circuit to HBM and clears
+  // them (one FP64 atomic per gate and group).
+  __device__ __forceinline__ void flush() {
+    fold();
+    for (int gi = p.tid; gi < p.P.n_gates; gi += p.T) {
+      const double sum = gsum[gi];
+      gsum[gi] = 0.0;
+      const int32_t slot = p.P.gate[gi].slot;
+      if (slot >= 0 && sum != 0.0)
+        atomicAdd(&grad_acc[p.circ * p.n_params + slot], sum * (double)p.P.gate[gi].coef);
+    }
+  }
+
+  __device__ __forceinline__ bool next() {
+    const int64_t prev = p.circ;
+    const int r = p.advance();
+    if (r == 0) return false;
+    if (r == 2) {
+      if (prev >= 0 && p.P.n_grad) {
+        const int64_t c = p.circ;
+        p.circ = prev;
+        flush();
+        p.circ = c;
+      }
+      p.build_mats();
+    }
+    return true;
+  }
+
+  // tile orders as in FwdPass
+  __device__ __forceinline__ void load(int f, bool raw) {
+    const Phase& ph = p.P.phase[f];
     bu = 0;
     for (int b = 0; b < ph.ntid; ++b)
-      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+      if ((p.tid >> b) & 1) bu ^= ph.tid_off[b];
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
-      regs_ld(a, j, tp[bu ^ ph.reg_off[j]]);
-      regs_ld(l, j, tl[bu ^ ph.reg_off[j]]);
+      if (raw) {
+        regs_ld_raw(a, j, p.tile[bu ^ ph.reg_off[j]]);
+        regs_ld_raw(l, j, p.tile[p.half + (bu ^ ph.reg_off[j])]);
+      } else {
+        regs_ld(a, j, p.tile[bu ^ ph.reg_off[j]]);
+        regs_ld(l, j, p.tile[p.half + (bu ^ ph.reg_off[j])]);
+      }
     }
   }
 
-  __device__ __forceinline__ void end(int f) {
-    const Phase& ph = P.phase[f];
+  __device__ __forceinline__ void store(int f, bool raw) {
+    const Phase& ph = p.P.phase[f];
 #pragma unroll
     for (int j = 0; j < NU; ++j) {
-      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
-      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
+      p.tile[bu ^ ph.reg_off[j]] = raw ? regs_st_raw(a, j) : regs_st(a, j);
+      p.tile[p.half + (bu ^ ph.reg_off[j])] = raw ? regs_st_raw(l, j) : regs_st(l, j);
     }
-    __syncthreads();
+  }
+
+  __device__ __forceinline__ void begin(int f) { load(f, false); }
+  __device__ __forceinline__ void begin_first(int f) { load(f, true); }
+
+  __device__ __forceinline__ void end(int f) {
+    store(f, false);
+    group_sync(p.bar, p.T);
+  }
+
+  __device__ __forceinline__ void end_last(int f) {
+    store(f, true);
+    group_sync(p.bar, p.T);
   }
 
   // end of a phase whose successor is warp-local (Phase::wlocal)
   __device__ __forceinline__ void end_w(int f) {
-    const Phase& ph = P.phase[f];
-#pragma unroll
-    for (int j = 0; j < NU; ++j) {
-      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
-      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
-    }
+    store(f, false);
     __syncwarp();
   }
 
-  // Warp-reduce one gate's partial gradient into this warp's slot of gate g
-  // (each slot is written by one lane of one warp: no atomics).
+  // Warp-reduce one gate's partial gradient into this warp's sum of gate g
+  // (each sum is updated by one lane of one warp: no atomics).
   __device__ __forceinline__ void grad(int g, real part) {
 #pragma unroll
     for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-    if ((tid & 31) == 0) gacc[(tid >> 5) * kMaxPassGates + g] = part;
+    if ((p.tid & 31) == 0) gacc[(p.tid >> 5) * ng + g] += part;
   }
 
   // Eight gates at once: a transposed butterfly leaves the warp sum of value
@@ -1260,7 +1573,7 @@ struct BwdPass {
   // marks an unused value.
   __device__ __forceinline__ void grad8(real v0, real v1, real v2, real v3, real v4, real v5, real v6, real v7,
                                         int g0, int g1, int g2, int g3, int g4, int g5, int g6, int g7) {
-    const unsigned lane = tid & 31;
+    const unsigned lane = p.tid & 31;
     real v[8] = {v0, v1, v2, v3, v4, v5, v6, v7};
     const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
 #pragma unroll
@@ -1289,34 +1602,27 @@ struct BwdPass {
 #pragma unroll
       for (int j = 1; j < 8; ++j)
         if (which == j) g = gs[j];
-      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = v[0];
+      if (g >= 0) gacc[(p.tid >> 5) * ng + g] += v[0];
     }
   }
 
   __device__ __forceinline__ void dense(int f) {
-    dense_phase<real>(P, P.phase[f], tp, tid, blockDim.x);
-    dense_phase<real>(P, P.phase[f], tl, tid, blockDim.x);
-    __syncthreads();
+    dense_phase<real>(p.P, p.P.phase[f], p.tile, p.tid, p.T);
+    dense_phase<real>(p.P, p.P.phase[f], p.tile + p.half, p.tid, p.T);
+    group_sync(p.bar, p.T);
+  }
+  __device__ __forceinline__ void to_planar() { p.convert(true); }
+  __device__ __forceinline__ void to_raw() { p.convert(false); }
+
+  // the last phase ended with a group barrier: the partials may be folded
+  __device__ __forceinline__ void finish() {
+    if (p.P.n_grad && ++since_fold == kFoldTiles) fold();
+    p.write_back(nullptr);
   }
 
-  __device__ __forceinline__ void finish() {
-#pragma unroll
-    for (int k = 0; k < NU; ++k) {
-      const uint64_t g = (gthr | P.gk[k]) >> E;
-      reinterpret_cast<U*>(sp)[g] = from_s(tp[sthr ^ P.sk[k]]);
-      reinterpret_cast<U*>(sl)[g] = from_s(tl[sthr ^ P.sk[k]]);
-    }
-    if (P.n_grad) {
-      __syncthreads();
-      const int nw = blockDim.x >> 5;
-      for (int g = tid; g < P.n_gates; g += blockDim.x) {
-        const int32_t slot = P.gate[g].slot;
-        if (slot < 0) continue;
-        double sum = 0.0;
-        for (int w = 0; w < nw; ++w) sum += (double)gacc[w * kMaxPassGates + g];
-        atomicAdd(&grad_acc[circ * n_params + slot], sum * (double)P.gate[g].coef);
-      }
-    }
+  __device__ __forceinline__ void close() {
+    if (p.circ >= 0 && p.P.n_grad) flush();
+    cp_async_wait_all();
   }
 };
 
@@ -1325,27 +1631,16 @@ struct BwdPass {
 
 // Kernel prologues shared by the generic and the generated pass kernels.
 // Generic (interpreted) kernels: plain matrices for the normalised rotations.
-#define TEDQ_FWD_PROLOGUE_GENERIC(REAL, RB)                                                          \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
-                                 psi, params, n_params, init, circ0, false);
-#define TEDQ_BWD_PROLOGUE_GENERIC(REAL, RB)                                                          \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  __shared__ REAL tedq_gacc[8 * tedq::kMaxPassGates];                                                \
-  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
-                                 tedq_gacc, psi, lam, params, n_params, grad_acc, circ0, false);
+#define TEDQ_FWD_PROLOGUE_GENERIC(REAL, RB)                                                             \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  tedq::dev::FwdPass<REAL, RB> c(P, tedq_smem_raw, psi, params, n_params, init, n_tiles, false);
+#define TEDQ_BWD_PROLOGUE_GENERIC(REAL, RB)                                                             \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  tedq::dev::BwdPass<REAL, RB> c(P, tedq_smem_raw, psi, lam, params, n_params, grad_acc, n_tiles, false);
 
-#define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                  \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  tedq::dev::FwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
-                                 psi, params, n_params, init, circ0);
-
-#define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                  \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                     \
-  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                      \
-  __shared__ REAL tedq_gacc[8 * tedq::kMaxPassGates];                                                    \
-  tedq::dev::BwdPass<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats, \
-                                 tedq_gacc, psi, lam, params, n_params, grad_acc, circ0);
+#define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                     \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  tedq::dev::FwdPass<REAL, RB> c(P, tedq_smem_raw, psi, params, n_params, init, n_tiles);
+#define TEDQ_BWD_PROLOGUE(REAL, RB)                                                                     \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  tedq::dev::BwdPass<REAL, RB> c(P, tedq_smem_raw, psi, lam, params, n_params, grad_acc, n_tiles);

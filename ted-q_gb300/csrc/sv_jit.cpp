@@ -73,34 +73,25 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
 static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
-  // as many CTAs per SM as their shared memory (tile + matrices + gradient
-  // slots) allows while every thread may keep 128 registers;
-  // TEDQ_GB300_CTAS=<f><b> (digits, e.g. 23) asks for f forward and b adjoint
-  // CTAs per SM instead (fewer registers per thread): a tuning knob for
-  // measurements
-  const int threads = 1 << (P.m - P.R);
-  const int tile_bytes = (adjoint ? 32 : 16) << (P.m - P.e);
-  const int rsize = P.e == 1 ? 4 : 8;
-  const int static_bytes = adjoint ? 5 * 1024 + (threads / 32) * kMaxPassGates * rsize : 5 * 1024;
-  const int by_smem = (227 * 1024) / (tile_bytes + static_bytes + 1024);
-  int min_blocks = std::min(by_smem, 65536 / (threads * 128));
-  if (const char* env = getenv("TEDQ_GB300_CTAS"))
-    if (strlen(env) == 2 && env[adjoint ? 1 : 0] >= '1' && env[adjoint ? 1 : 0] <= '8')
-      min_blocks = std::min(by_smem, env[adjoint ? 1 : 0] - '0');
-  min_blocks = std::max(1, std::min(min_blocks, 8));
+  // one CTA of G thread groups and G + 1 tile slots (pipe_layout); as many
+  // CTAs per SM as the shared memory allows
+  const int G = pipe_groups(P, adjoint);
+  const int threads = G << (P.m - P.R);
+  const int by_smem = (int)(kPipeSmemMax / (pipe_layout(P, G, adjoint).total + 1024));
+  const int min_blocks = std::max(1, std::min(by_smem, 65536 / (threads * 128)));
   if (!adjoint) {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
-             "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long circ0) {\n"
-             "  TEDQ_FWD_PROLOGUE(%s, %d)\n",
+             "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long n_tiles) {\n"
+             "  TEDQ_FWD_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
              threads, min_blocks, index, real, real, real, real, P.R);
   } else {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_bwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
-             "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long circ0) {\n"
-             "  TEDQ_BWD_PROLOGUE(%s, %d)\n",
+             "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long n_tiles) {\n"
+             "  TEDQ_BWD_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
              threads, min_blocks, index, real, real, real, real, P.R);
   }
   o << buf;
@@ -118,11 +109,14 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
   int kap = -1;  // last normalised matrix applied (its [2].x = scale so far)
   for (int f = 0; f < P.n_phases; ++f) {
     const Phase& ph = P.phase[f];
+    const bool last = f + 1 == P.n_phases;
     if (ph.type != PH_REG) {
+      if (f == 0) o << "  c.to_planar();\n";
       o << "  c.dense(" << f << ");\n";
+      if (last) o << "  c.to_raw();\n";
       continue;
     }
-    o << "  c.begin(" << f << ");\n";
+    o << (f == 0 ? "  c.begin_first(" : "  c.begin(") << f << ");\n";
     for (int g = ph.g0; g < ph.g1; ++g) {
       const RGate& r = P.gate[g];
       if (adjoint && r.grad != GR_NONE) {
@@ -150,10 +144,10 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
       if (adjoint) o << "  rescale<" << (int)P.R << ">(c.l, c.mats[" << (int)P.norm_last << "][2].x);\n";
       kap = -1;
     }
-    const bool next_wl = f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal;
-    o << (next_wl ? "  c.end_w(" : "  c.end(") << f << ");\n";
+    const bool next_wl = !last && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal;
+    o << (last ? "  c.end_last(" : next_wl ? "  c.end_w(" : "  c.end(") << f << ");\n";
   }
-  o << "  c.finish();\n}\n\n";
+  o << "  c.finish();\n  }\n  c.close();\n}\n\n";
 }
 
 std::vector<JitSource> jit_sources(const Program& p) {
@@ -364,6 +358,7 @@ struct Driver {
   decltype(&cuModuleGetFunction) get = nullptr;
   decltype(&cuFuncSetAttribute) set_attr = nullptr;
   decltype(&cuLaunchKernel) launch = nullptr;
+  decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
 };
 
 template <typename F>
@@ -382,7 +377,8 @@ bool entry(const char* name, F& fn, std::string& why) {
 Driver load_driver() {
   Driver d;
   if (!entry("cuModuleLoadData", d.load, d.why) || !entry("cuModuleGetFunction", d.get, d.why) ||
-      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why))
+      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why) ||
+      !entry("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy, d.why))
     return d;
   d.ok = true;
   return d;
@@ -394,8 +390,6 @@ Driver& driver() {
   std::call_once(once, [] { d = load_driver(); });
   return d;
 }
-
-constexpr int kMaxGridY = 65535;
 
 }  // namespace
 
@@ -428,7 +422,7 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
       err = "missing kernel " + srcs[i].name;
       return false;
     }
-    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 200 * 1024);
+    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)kPipeSmemMax);
     ((int)i < n_fwd ? out.fwd : out.bwd).push_back(reinterpret_cast<void*>(f));
   }
   return true;
@@ -436,36 +430,47 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
 
 static cudaError_t to_rt(CUresult r) { return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure; }
 
+// Persistent grid: as many CTAs as fit on the device at once, at most one per tile.
+static cudaError_t jit_grid(CUfunction f, int threads, unsigned smem, int64_t n_tiles, unsigned& grid) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  if (driver().occupancy(&per_sm, f, threads, smem) != CUDA_SUCCESS || per_sm < 1)
+    return cudaErrorInvalidConfiguration;
+  const int64_t want = (int64_t)sms * per_sm;
+  grid = (unsigned)(n_tiles < want ? n_tiles : want);
+  return cudaSuccess;
+}
+
 cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
                            const void* init, int64_t batch, cudaStream_t s) {
-  const int E = dbl ? 0 : 1;
-  const unsigned smem = 16u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
-  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
-    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    long long circ0 = c0;
-    void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
-                    const_cast<void**>(&init), &circ0};
-    CUresult r = driver().launch(reinterpret_cast<CUfunction>(fn), tiles, (unsigned)nb, 1, T, 1, 1, smem,
-                                 reinterpret_cast<CUstream>(s), args, nullptr);
-    if (r != CUDA_SUCCESS) return to_rt(r);
-  }
-  return cudaSuccess;
+  (void)dbl;
+  const int G = pipe_groups(P, false);
+  const unsigned smem = pipe_layout(P, G, false).total, T = (unsigned)G << (P.m - P.R);
+  long long n_tiles = (long long)(batch << (P.n - P.m));
+  CUfunction f = reinterpret_cast<CUfunction>(fn);
+  unsigned grid = 0;
+  cudaError_t e = jit_grid(f, (int)T, smem, n_tiles, grid);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
+                  const_cast<void**>(&init), &n_tiles};
+  return to_rt(driver().launch(f, grid, 1, 1, T, 1, 1, smem, reinterpret_cast<CUstream>(s), args, nullptr));
 }
 
 cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
                            int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
-  const int E = dbl ? 0 : 1;
-  const unsigned smem = 32u << (P.m - E), T = 1u << (P.m - P.R), tiles = 1u << (P.n - P.m);
-  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
-    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    long long circ0 = c0;
-    void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
-                    &circ0};
-    CUresult r = driver().launch(reinterpret_cast<CUfunction>(fn), tiles, (unsigned)nb, 1, T, 1, 1, smem,
-                                 reinterpret_cast<CUstream>(s), args, nullptr);
-    if (r != CUDA_SUCCESS) return to_rt(r);
-  }
-  return cudaSuccess;
+  (void)dbl;
+  const int G = pipe_groups(P, true);
+  const unsigned smem = pipe_layout(P, G, true).total, T = (unsigned)G << (P.m - P.R);
+  long long n_tiles = (long long)(batch << (P.n - P.m));
+  CUfunction f = reinterpret_cast<CUfunction>(fn);
+  unsigned grid = 0;
+  cudaError_t e = jit_grid(f, (int)T, smem, n_tiles, grid);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
+                  &n_tiles};
+  return to_rt(driver().launch(f, grid, 1, 1, T, 1, 1, smem, reinterpret_cast<CUstream>(s), args, nullptr));
 }
 
 }  // namespace tedq

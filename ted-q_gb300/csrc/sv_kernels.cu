@@ -6,13 +6,15 @@
 // that loop (``back_prop``, :142-144).
 //
 // Kernels
-//   fwd_pass_kernel  one HBM pass of the forward schedule: a CTA stages one
-//                    tile (2^m amplitudes, 64 KiB) in shared memory, runs the
-//                    pass's register phases, writes the tile back in place.
-//   bwd_pass_kernel  one pass of the adjoint sweep over psi and lambda at once:
-//                    for every parameterised gate (in reverse order) it adds
-//                    coef * Im<lambda|G|psi> into the gradient, then applies the
-//                    inverse gate to both states.
+//   fwd_pass_kernel  one HBM pass of the forward schedule: persistent CTAs,
+//                    two thread groups each running the pass's register phases
+//                    on one tile (2^m amplitudes, 64 KiB) in shared memory
+//                    while the next tile streams into a third slot; tiles are
+//                    written back in place.
+//   bwd_pass_kernel  one pass of the adjoint sweep over psi and lambda at once
+//                    (same pipeline): for every parameterised gate (in reverse
+//                    order) it adds coef * Im<lambda|G|psi> into the gradient,
+//                    then applies the inverse gate to both states.
 //   expval_kernel    Pauli-string expectations, one read of the state,
 //                    FP32 partial sums per thread/warp and FP64 across warps/CTAs.
 //   probs kernels, lambda_init_kernel, finalize kernels.
@@ -51,50 +53,67 @@ constexpr int kE = dev::UnitsPerAmp<real>::E;
 // Normalised rotations run with their plain matrices here (no pass scale).
 
 template <typename real, int R>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(512, 1)
     fwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi,
                     const real* __restrict__ params, int n_params, const cpx<real>* __restrict__ init,
-                    int64_t circ0) {
+                    int64_t n_tiles) {
   TEDQ_FWD_PROLOGUE_GENERIC(real, R)
-  for (int f = 0; f < P.n_phases; ++f) {
-    const Phase& ph = P.phase[f];
-    if (ph.type == PH_REG) {
-      c.begin(f);
-      for (int g = ph.g0; g < ph.g1; ++g) {
-        const RGate& r = P.gate[g];
-        dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
+  while (c.next()) {
+    for (int f = 0; f < P.n_phases; ++f) {
+      const Phase& ph = P.phase[f];
+      const bool last = f + 1 == P.n_phases;
+      if (ph.type == PH_REG) {
+        if (f == 0) c.begin_first(f);
+        else c.begin(f);
+        for (int g = ph.g0; g < ph.g1; ++g) {
+          const RGate& r = P.gate[g];
+          dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
+        }
+        if (last) c.end_last(f);
+        else if (P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
+        else c.end(f);
+      } else {
+        if (f == 0) c.to_planar();
+        c.dense(f);
+        if (last) c.to_raw();
       }
-      if (f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
-      else c.end(f);
-    } else {
-      c.dense(f);
     }
+    c.finish();
   }
-  c.finish();
+  c.close();
 }
 
 template <typename real, int R>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(512, 1)
     bwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi, cpx<real>* __restrict__ lam,
-                    const real* __restrict__ params, int n_params, double* __restrict__ grad_acc, int64_t circ0) {
+                    const real* __restrict__ params, int n_params, double* __restrict__ grad_acc,
+                    int64_t n_tiles) {
   TEDQ_BWD_PROLOGUE_GENERIC(real, R)
-  for (int f = 0; f < P.n_phases; ++f) {
-    const Phase& ph = P.phase[f];
-    if (ph.type == PH_REG) {
-      c.begin(f);
-      for (int g = ph.g0; g < ph.g1; ++g) {
-        const RGate& r = P.gate[g];
-        if (r.grad != GR_NONE) c.grad(g, dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask));
-        dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
-        dev::apply_rgate<R, real>(r, c.l, c.mats[r.mat]);
+  while (c.next()) {
+    for (int f = 0; f < P.n_phases; ++f) {
+      const Phase& ph = P.phase[f];
+      const bool last = f + 1 == P.n_phases;
+      if (ph.type == PH_REG) {
+        if (f == 0) c.begin_first(f);
+        else c.begin(f);
+        for (int g = ph.g0; g < ph.g1; ++g) {
+          const RGate& r = P.gate[g];
+          if (r.grad != GR_NONE) c.grad(g, dev::dispatch_grad<R, real>(r.grad, r.k0, c.a, c.l, r.cmask));
+          dev::apply_rgate<R, real>(r, c.a, c.mats[r.mat]);
+          dev::apply_rgate<R, real>(r, c.l, c.mats[r.mat]);
+        }
+        if (last) c.end_last(f);
+        else if (P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
+        else c.end(f);
+      } else {
+        if (f == 0) c.to_planar();
+        c.dense(f);
+        if (last) c.to_raw();
       }
-      if (f + 1 < P.n_phases && P.phase[f + 1].type == PH_REG && P.phase[f + 1].wlocal) c.end_w(f);
-      else c.end(f);
-    } else {
-      c.dense(f);
     }
+    c.finish();
   }
-  c.finish();
+  c.close();
 }
 
 template <typename real>
@@ -435,44 +454,55 @@ cudaError_t ensure_smem(K kernel, size_t bytes) {
   return e;
 }
 
+// Persistent grid of a pass kernel: as many CTAs as fit on the device at
+// once (at most one per tile).
+template <typename K>
+cudaError_t pass_grid(K kernel, int threads, size_t smem, int64_t n_tiles, unsigned& grid) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int64_t want = (int64_t)sms * per_sm;
+  grid = (unsigned)(n_tiles < want ? n_tiles : want);
+  return cudaSuccess;
+}
+
 template <typename real, int R>
 cudaError_t fwd_impl(const PassParams& P, void* psi, const void* params, int n_params, const void* init,
                      int64_t batch, cudaStream_t s) {
-  constexpr int E = kE<real>;
-  const size_t smem = (size_t)16 << (P.m - E);
+  const int G = pipe_groups(P, false);
+  const size_t smem = pipe_layout(P, G, false).total;
+  if (smem > kPipeSmemMax) return cudaErrorInvalidConfiguration;
   auto kern = fwd_pass_kernel<real, R>;
   cudaError_t e = ensure_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  const int T = 1 << (P.m - R);
-  const unsigned tiles = 1u << (P.n - P.m);
-  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
-    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    dim3 grid(tiles, (unsigned)nb);
-    e = launch_kernel(kern, grid, dim3(T), smem, s, P, static_cast<cpx<real>*>(psi),
-                      static_cast<const real*>(params), n_params, static_cast<const cpx<real>*>(init), c0);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  const int threads = G << (P.m - R);
+  const int64_t n_tiles = batch << (P.n - P.m);
+  unsigned grid = 0;
+  e = pass_grid(kern, threads, smem, n_tiles, grid);
+  if (e != cudaSuccess) return e;
+  return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
+                       static_cast<const real*>(params), n_params, static_cast<const cpx<real>*>(init), n_tiles);
 }
 
 template <typename real, int R>
 cudaError_t bwd_impl(const PassParams& P, void* psi, void* lam, const void* params, int n_params,
                      double* grad_acc, int64_t batch, cudaStream_t s) {
-  constexpr int E = kE<real>;
-  const size_t smem = (size_t)32 << (P.m - E);
+  const int G = pipe_groups(P, true);
+  const size_t smem = pipe_layout(P, G, true).total;
+  if (smem > kPipeSmemMax) return cudaErrorInvalidConfiguration;
   auto kern = bwd_pass_kernel<real, R>;
   cudaError_t e = ensure_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  const int T = 1 << (P.m - R);
-  const unsigned tiles = 1u << (P.n - P.m);
-  for (int64_t c0 = 0; c0 < batch; c0 += kMaxGridY) {
-    const int64_t nb = batch - c0 < kMaxGridY ? batch - c0 : kMaxGridY;
-    dim3 grid(tiles, (unsigned)nb);
-    e = launch_kernel(kern, grid, dim3(T), smem, s, P, static_cast<cpx<real>*>(psi), static_cast<cpx<real>*>(lam),
-                      static_cast<const real*>(params), n_params, grad_acc, c0);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  const int threads = G << (P.m - R);
+  const int64_t n_tiles = batch << (P.n - P.m);
+  unsigned grid = 0;
+  e = pass_grid(kern, threads, smem, n_tiles, grid);
+  if (e != cudaSuccess) return e;
+  return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
+                       static_cast<cpx<real>*>(lam), static_cast<const real*>(params), n_params, grad_acc, n_tiles);
 }
 
 template <typename real>

@@ -25,6 +25,7 @@ typedef int int32_t;
 typedef long long int64_t;
 #else
 #include <stdint.h>
+#include <stdlib.h>
 #endif
 
 namespace tedq {
@@ -163,13 +164,61 @@ struct PassParams {
   CD fixed[kMaxFixed];
 };
 
+#if defined(__CUDACC__)
+#define TEDQ_HD __host__ __device__
+#else
+#define TEDQ_HD
+#endif
+
+// Shared memory of a pass kernel.  A CTA runs G thread groups of 2^(m-R)
+// threads; each group works on one tile at a time and the CTA holds G + 1
+// tile slots, so that while the groups compute, the next tile is already
+// arriving in the spare slot by asynchronous copies.  After the slots: per
+// group the pass matrices and (adjoint) the gradient sums, then one mbarrier
+// per slot.
+struct PipeLayout {
+  uint32_t slot_bytes, mats_off, gacc_off, mbar_off, total;
+};
+
+constexpr uint32_t kPipeSmemMax = 227u * 1024u;
+
+TEDQ_HD inline PipeLayout pipe_layout(const PassParams& P, int G, bool adjoint) {
+  PipeLayout L;
+  const uint32_t amp = P.e == 1 ? 8u : 16u;  // bytes per amplitude (complex64 / complex128)
+  const uint32_t T = 1u << (P.m - P.R);
+  const uint32_t W = T >= 32u ? T / 32u : 1u;
+  L.slot_bytes = (adjoint ? 2u : 1u) * (amp << P.m);
+  uint32_t off = L.slot_bytes * (uint32_t)(G + 1);
+  L.mats_off = off;
+  off += (uint32_t)G * (uint32_t)(P.n_mats > 0 ? P.n_mats : 1) * 4u * amp;
+  off = (off + 15u) & ~15u;
+  L.gacc_off = off;
+  // FP64 sums [G][gates], then per-warp partials [G][W][gates] in the state's precision
+  if (adjoint) off += (uint32_t)G * (uint32_t)(P.n_gates > 0 ? P.n_gates : 1) * (8u + W * (amp / 2u));
+  off = (off + 15u) & ~15u;
+  L.mbar_off = off;
+  off += 8u * (uint32_t)(G + 1);
+  L.total = off;
+  return L;
+}
+
+#if !defined(__CUDACC_RTC__)
+// Two groups (three slots) when they fit in shared memory, else one group
+// with a double-buffered tile; TEDQ_GB300_PIPE_GROUPS=1 asks for one group (a
+// measurement knob).
+inline int pipe_groups(const PassParams& P, bool adjoint) {
+  const uint32_t T = 1u << (P.m - P.R);
+  const char* env = getenv("TEDQ_GB300_PIPE_GROUPS");
+  const int want = (env && env[0] == '1') ? 1 : 2;
+  if (want == 2 && 2u * T <= 1024u && pipe_layout(P, 2, adjoint).total <= kPipeSmemMax) return 2;
+  return 1;
+}
+#endif
+
 // Unit-level shared-memory swizzle: the 16-byte unit u of a tile is stored at
 // u ^ fold3(u >> 3) where fold3 xors the 3-bit groups.  The map is linear over
 // GF(2), so offsets of disjoint bit sets combine with XOR.
-#if defined(__CUDACC__)
-__host__ __device__
-#endif
-inline uint32_t swz_unit(uint32_t u) {
+TEDQ_HD inline uint32_t swz_unit(uint32_t u) {
   uint32_t v = u >> 3, f = 0;
   while (v) { f ^= v & 7u; v >>= 3; }
   return u ^ f;

@@ -156,6 +156,33 @@ def test_alone_equals_in_batch():
     torch.testing.assert_close(again, batch, atol=1e-7, rtol=1e-7)
 
 
+@pytest.mark.parametrize("jit", [-1, 1], ids=["generic", "specialised"])
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+def test_gradients_alone_equal_in_batch(precision, jit):
+    """The pass kernels are persistent: each CTA takes a contiguous range of
+    tiles that starts and ends inside circuits, its two thread groups take
+    alternate tiles, and gradient partials are flushed per circuit.  A batch
+    of 37 circuits of 16 qubits (16 adjoint tiles each, about 4 per CTA) must
+    give every row the values and gradients it gets alone."""
+    spec = _vqc_spec(16, 2, seed=9)
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=jit, precision=precision)
+    if jit == 1:
+        assert cc._prog.jit_wait() is None
+    rdt = _rdt(precision)
+    gen = torch.Generator().manual_seed(9)
+    params = (torch.rand(37, cc.num_params, generator=gen, dtype=torch.float64) * 2 * np.pi).to(DEV, rdt)
+    pb = params.clone().requires_grad_(True)
+    out = cc.execute_batch(pb)
+    out.sum().backward()
+    tol = dict(atol=1e-12, rtol=1e-12) if precision == "c128" else dict(atol=2e-6, rtol=1e-5)
+    for b in (0, 1, 18, 36):
+        pa = params[b:b + 1].clone().requires_grad_(True)
+        alone = cc.execute_batch(pa)
+        alone.sum().backward()
+        torch.testing.assert_close(alone[0], out[b].detach(), **tol)
+        torch.testing.assert_close(pa.grad[0], pb.grad[b], **tol)
+
+
 def test_unfused_equals_fused():
     spec = _vqc_spec(11, 2, seed=5)
     a = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)
