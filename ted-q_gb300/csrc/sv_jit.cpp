@@ -19,6 +19,7 @@
 #include <sstream>
 #include <thread>
 
+#include "sv_kernels.cuh"
 #include "sv_program.h"
 
 namespace tedq {
@@ -430,17 +431,9 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
 
 static cudaError_t to_rt(CUresult r) { return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure; }
 
-// Persistent grid: as many CTAs as fit on the device at once, at most one per tile.
-static cudaError_t jit_grid(CUfunction f, int threads, unsigned smem, int64_t n_tiles, unsigned& grid) {
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  if (driver().occupancy(&per_sm, f, threads, smem) != CUDA_SUCCESS || per_sm < 1)
-    return cudaErrorInvalidConfiguration;
-  const int64_t want = (int64_t)sms * per_sm;
-  grid = (unsigned)(n_tiles < want ? n_tiles : want);
-  return cudaSuccess;
+static cudaError_t driver_residency(const void* key, int threads, size_t smem, int* per_sm) {
+  CUfunction f = reinterpret_cast<CUfunction>(const_cast<void*>(key));
+  return driver().occupancy(per_sm, f, threads, smem) == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidConfiguration;
 }
 
 cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
@@ -451,7 +444,7 @@ cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, c
   long long n_tiles = (long long)(batch << (P.n - P.m));
   CUfunction f = reinterpret_cast<CUfunction>(fn);
   unsigned grid = 0;
-  cudaError_t e = jit_grid(f, (int)T, smem, n_tiles, grid);
+  cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
                   const_cast<void**>(&init), &n_tiles};
@@ -466,7 +459,7 @@ cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, v
   long long n_tiles = (long long)(batch << (P.n - P.m));
   CUfunction f = reinterpret_cast<CUfunction>(fn);
   unsigned grid = 0;
-  cudaError_t e = jit_grid(f, (int)T, smem, n_tiles, grid);
+  cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
                   &n_tiles};

@@ -24,6 +24,7 @@
 // register work per amplitude is 4-8 FMA per gate.
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 #include <tuple>
 #include <type_traits>
@@ -454,19 +455,10 @@ cudaError_t ensure_smem(K kernel, size_t bytes) {
   return e;
 }
 
-// Persistent grid of a pass kernel: as many CTAs as fit on the device at
-// once (at most one per tile).
 template <typename K>
-cudaError_t pass_grid(K kernel, int threads, size_t smem, int64_t n_tiles, unsigned& grid) {
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const int64_t want = (int64_t)sms * per_sm;
-  grid = (unsigned)(n_tiles < want ? n_tiles : want);
-  return cudaSuccess;
+cudaError_t runtime_residency(const void* key, int threads, size_t smem, int* per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, reinterpret_cast<K>(const_cast<void*>(key)), threads,
+                                                       smem);
 }
 
 template <typename real, int R>
@@ -481,7 +473,8 @@ cudaError_t fwd_impl(const PassParams& P, void* psi, const void* params, int n_p
   const int threads = G << (P.m - R);
   const int64_t n_tiles = batch << (P.n - P.m);
   unsigned grid = 0;
-  e = pass_grid(kern, threads, smem, n_tiles, grid);
+  e = pass_grid_cached(reinterpret_cast<const void*>(kern), threads, smem, n_tiles, runtime_residency<decltype(kern)>,
+                       grid);
   if (e != cudaSuccess) return e;
   return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
                        static_cast<const real*>(params), n_params, static_cast<const cpx<real>*>(init), n_tiles);
@@ -499,7 +492,8 @@ cudaError_t bwd_impl(const PassParams& P, void* psi, void* lam, const void* para
   const int threads = G << (P.m - R);
   const int64_t n_tiles = batch << (P.n - P.m);
   unsigned grid = 0;
-  e = pass_grid(kern, threads, smem, n_tiles, grid);
+  e = pass_grid_cached(reinterpret_cast<const void*>(kern), threads, smem, n_tiles, runtime_residency<decltype(kern)>,
+                       grid);
   if (e != cudaSuccess) return e;
   return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
                        static_cast<cpx<real>*>(lam), static_cast<const real*>(params), n_params, grad_acc, n_tiles);
@@ -573,6 +567,41 @@ cudaError_t lambda_impl(int n, const TermTable& TT, const ProbsTable& PT, const 
 }
 
 }  // namespace
+
+cudaError_t pass_grid_cached(const void* key, int threads, size_t smem, int64_t n_tiles,
+                             cudaError_t (*query)(const void* key, int threads, size_t smem, int* per_sm),
+                             unsigned& grid) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, int, size_t>, int> resident;  // (kernel, device, threads, smem)
+  static int sm_count[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0, sms = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = resident.find(std::make_tuple(key, dev, threads, smem));
+    if (it != resident.end()) per_sm = it->second;
+    if (dev >= 0 && dev < 64) sms = sm_count[dev];
+  }
+  if (sms == 0) {
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  if (per_sm == 0) {
+    e = query(key, threads, smem, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  }
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    resident[std::make_tuple(key, dev, threads, smem)] = per_sm;
+    if (dev >= 0 && dev < 64) sm_count[dev] = sms;
+  }
+  const int64_t want = (int64_t)sms * per_sm;
+  grid = (unsigned)(n_tiles < want ? n_tiles : want);
+  return cudaSuccess;
+}
 
 cudaError_t launch_fwd_pass(bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
                             const void* init, int64_t batch, cudaStream_t s) {

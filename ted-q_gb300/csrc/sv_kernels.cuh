@@ -51,6 +51,16 @@ struct ProbsTable {
 };
 
 // Forward pass over a batch: psi [batch][2^n]; params [batch][n_params].
+// Persistent grid of a pass kernel: as many CTAs as fit on the current device
+// at once, at most one per tile.  `query` returns the resident CTAs per SM of
+// the kernel (key) at the given block size and dynamic shared memory; its
+// answer and the SM count are cached per device, so that only the first
+// launch of a kernel shape makes runtime queries (later launches may run
+// inside stream capture).
+cudaError_t pass_grid_cached(const void* key, int threads, size_t smem, int64_t n_tiles,
+                             cudaError_t (*query)(const void* key, int threads, size_t smem, int* per_sm),
+                             unsigned& grid);
+
 cudaError_t launch_fwd_pass(bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
                             const void* init, int64_t batch, cudaStream_t s);
 // Adjoint pass: uncomputes psi and lambda through the pass's gates and adds

@@ -309,12 +309,20 @@ static uint8_t specialised_kind(const HGate& g, bool phase_free, bool norm);
 
 // Register-phase cost of a gate (packed FP32x2 instructions per amplitude of
 // one state): the fused form is kept only where it is cheaper than its parts.
-// A normalised rotation counts as 2: it executes one FFMA2 per component but
-// carries the code of both of its forms, and measured runs of RX RY RZ ran
-// faster fused (the pass kernels are sensitive to code size).
+// A normalised rotation counts as 1 (one FFMA2 per component): with the tile
+// pipeline, RX RY RZ as three normalised gates measured 3 % faster than the
+// fused dense 2x2 in the forward passes (96.9 -> 93.8 ms per step on the
+// 20-qubit VQC; with one tile per CTA the fused form had been faster, the
+// kernels then being more sensitive to code size).
+// TEDQ_GB300_NORM_COST=<1..4> overrides the 1 (a measurement knob).
+static int norm_cost() {
+  const char* env = getenv("TEDQ_GB300_NORM_COST");
+  return (env && env[0] >= '1' && env[0] <= '4' && !env[1]) ? env[0] - '0' : 1;
+}
+
 static int gate_cost(const HGate& g, bool norm) {
   if (g.kind == GK_X || g.kind == GK_SWAP) return 0;
-  if (normalised_kind(g, norm)) return 2;
+  if (normalised_kind(g, norm)) return norm_cost();
   if (g.kind == GK_D1) return (norm && g.cmask == 0) || specialised_kind(g, false, false) == GK_PH ? 1 : 2;
   if (is_hadamard(g)) return 2;
   if (g.factors.size() == 1 && (g.factors[0].op == F_RX || g.factors[0].op == F_RY)) return 2;

@@ -8,8 +8,9 @@ waits for the per-circuit kernel compile and never loads a kernel module
 These tests call it through the C ABI, twice in a row, and compare with
 tedq_run on the same inputs; a fresh 14-qubit program (specialised kernels on)
 is called first through tedq_run_noalloc, which must then run the generic
-kernels, load no module and still match the complex128 oracle.  The file is
-named to be collected last."""
+kernels, load no module and still match the complex128 oracle; and a call
+captured into a CUDA graph replays correctly.  The file is named to be
+collected last."""
 
 import ctypes
 
@@ -102,6 +103,45 @@ def test_noalloc_first_call_loads_no_module():
         torch.testing.assert_close(out2, ref_out, atol=1e-6, rtol=1e-6)
         torch.testing.assert_close(psi2, ref_psi, atol=1e-6, rtol=1e-6)
         torch.testing.assert_close(out2, out, atol=1e-5, rtol=1e-5)
+
+
+def test_noalloc_inside_cuda_graph_capture():
+    """The use the entry point exists for: a 14-qubit program with Pauli-string
+    outputs (specialised kernels loaded by a warm-up tedq_run, first
+    allocation-free call made before capture) is captured into a CUDA graph
+    through tedq_run_noalloc; replays with new parameters written into the
+    captured input buffer match tedq_run."""
+    _, cc = _circuit(n=14, jit=1, expval=True, seed=5)
+    assert cc._prog.jit_wait() is None
+    L = _lib.lib()
+    prog = cc._prog
+    gen = torch.Generator().manual_seed(17)
+    B = 4
+    P = (torch.rand(B, cc.num_params, generator=gen) * 2 * np.pi).to(DEV)
+    cc._forward(P)
+    torch.cuda.synchronize()
+    assert _modules_loaded(cc) > 0
+    _noalloc(cc, P)
+    psi = torch.empty((B, 1 << prog.ns), dtype=prog.cdtype, device=DEV)
+    out = torch.empty((B, prog.n_real), dtype=prog.rdtype, device=DEV)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            st = L.tedq_run_noalloc(prog.handle, ctypes.c_void_p(P.data_ptr()), B, ctypes.c_void_p(psi.data_ptr()),
+                                    ctypes.c_void_p(out.data_ptr()), None,
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(st, "tedq_run_noalloc (captured)")
+    torch.cuda.current_stream().wait_stream(side)
+    for _ in range(2):
+        P.copy_((torch.rand(B, cc.num_params, generator=gen) * 2 * np.pi).to(DEV))
+        graph.replay()
+        torch.cuda.synchronize()
+        ref_out, ref_psi = cc._forward(P)
+        torch.cuda.synchronize()
+        torch.testing.assert_close(out, ref_out, atol=1e-6, rtol=1e-6)
+        torch.testing.assert_close(psi, ref_psi, atol=1e-6, rtol=1e-6)
 
 
 def test_noalloc_rejects_batch_beyond_static_scratch():
