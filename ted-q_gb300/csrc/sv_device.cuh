@@ -1138,24 +1138,23 @@ __device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_test(uint64_t* b, unsigned parity) {
+// One bounded wait step: the thread is suspended until the mbarrier phase of
+// the given parity completes or about a microsecond has passed.
+__device__ __forceinline__ bool mbar_try(uint64_t* b, unsigned parity) {
   uint32_t done;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(done)
-      : "r"(smem_addr(b)), "r"(parity)
+      : "r"(smem_addr(b)), "r"(parity), "r"(1000u)
       : "memory");
   return done != 0;
 }
 
 // Waits for the completion of the mbarrier phase of the given parity; gives
-// up after about half a second (2^21 polls, sleeping between the later ones)
-// and returns false.
+// up after 2^20 steps (about a second) and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
-  for (uint32_t i = 0; i < (1u << 21); ++i) {
-    if (mbar_test(b, parity)) return true;
-    if (i >= 32) __nanosleep(i < 1024 ? 32 : 256);
-  }
+  for (uint32_t i = 0; i < (1u << 20); ++i)
+    if (mbar_try(b, parity)) return true;
   return false;
 }
 
@@ -1208,11 +1207,8 @@ struct Pipe {
   C* lam;
   const real* params;
   int n_params;
-  int G, g, T, tid, bar;
+  int G, g, T, tid, bar, nslots;
   int64_t t0, cnt, k, circ;
-  uint64_t gth;    // thread part of the global staging offsets
-  uint32_t sthr;   // thread part of the shared-memory staging units
-  uint64_t gthr;   // current tile: global offset base of this thread
   C* st;           // current circuit's psi
   C* sl;           // current circuit's lambda
   bool ok;         // false once a slot wait gave up (outputs become NaN)
@@ -1226,6 +1222,7 @@ struct Pipe {
     g = (int)threadIdx.x / T;
     tid = (int)threadIdx.x - g * T;
     bar = 1 + g;
+    nslots = pipe_slots(P, G);
     const PipeLayout L = pipe_layout(P, G, ADJ);
     slots = reinterpret_cast<S*>(smem);
     su = L.slot_bytes >> 4;
@@ -1236,33 +1233,34 @@ struct Pipe {
     const int64_t per = n_tiles / gridDim.x, rem = n_tiles % gridDim.x, b = blockIdx.x;
     t0 = b * per + (b < rem ? b : rem);
     cnt = per + (b < rem ? 1 : 0);
-    gth = 0;
-    sthr = 0;
-    thread_offsets(P, tid, P.m - R, gth, sthr);
     if (threadIdx.x == 0)
-      for (int s = 0; s <= G; ++s) mbar_init(&mbar[s], (unsigned)T);
+      for (int s = 0; s < nslots; ++s) mbar_init(&mbar[s], (unsigned)T);
     k = g - G;
     circ = -1;
     ok = true;
     tile = slots;
     st = sl = nullptr;
-    gthr = 0;
   }
 
-  // First tiles: tile j < G + 1 is fetched by group (j + G - 1) % G, the group
-  // that fetches every later tile of its slot.  Call after the CTA barrier
-  // that publishes the mbarrier initialisation.
+  // First tiles: tile j < nslots is fetched by group (j + G - 1) % G, the
+  // group that fetches every later tile of its slot.  Call after the CTA
+  // barrier that publishes the mbarrier initialisation.
   __device__ __forceinline__ void start(const C* init) {
-    for (int j = 0; j <= G && j < cnt; ++j)
+    for (int j = 0; j < nslots && j < cnt; ++j)
       if ((j + G - 1) % G == g) fetch(j, init);
   }
 
   __device__ __forceinline__ void fetch(int64_t kk, const C* init) {
-    const int s = (int)(kk % (G + 1));
+    const int s = (int)(kk % nslots);
     S* dst = slots + (size_t)s * su;
     const int64_t gt = t0 + kk;
     const int64_t c = gt >> (P.n - P.m);
     const uint32_t tic = (uint32_t)(gt & ((1ll << (P.n - P.m)) - 1));
+    // staging offsets are recomputed per tile (not kept in registers across
+    // the register phases)
+    uint64_t gth = 0;
+    uint32_t sthr = 0;
+    thread_offsets(P, tid, P.m - R, gth, sthr);
     const uint64_t gb = tile_base(P, tic) | gth;
     const C* src = psi + (c << P.n);
     if (ADJ || P.init == 0) {
@@ -1283,22 +1281,25 @@ struct Pipe {
     }
   }
 
-  // Next tile of this group: waits for its slot; on a new circuit the caller
-  // rebuilds the matrices (returns 2), else returns 1; 0 = no tile left.
+  // Next tile of this group (slot not yet waited for): on a new circuit the
+  // caller rebuilds the matrices (returns 2) -- while the tile may still be
+  // arriving -- else returns 1; 0 = no tile left.
   __device__ __forceinline__ int advance() {
     k += G;
     if (k >= cnt) return 0;
-    const int s = (int)(k % (G + 1));
-    if (ok && !mbar_wait(&mbar[s], (unsigned)((k / (G + 1)) & 1))) ok = false;
-    tile = slots + (size_t)s * su;
+    tile = slots + (size_t)(k % nslots) * su;
     const int64_t gt = t0 + k;
     const int64_t c = gt >> (P.n - P.m);
-    gthr = tile_base(P, (uint32_t)(gt & ((1ll << (P.n - P.m)) - 1))) | gth;
     if (c == circ) return 1;
     circ = c;
     st = psi + (c << P.n);
     if (ADJ) sl = lam + (c << P.n);
     return 2;
+  }
+
+  // Waits for the current tile's copies.
+  __device__ __forceinline__ void arrive_wait() {
+    if (ok && !mbar_wait(&mbar[k % nslots], (unsigned)((k / nslots) & 1))) ok = false;
   }
 
   // Matrices of the current circuit (the previous tile's last group barrier
@@ -1320,8 +1321,13 @@ struct Pipe {
     group_sync(bar, T);
   }
 
-  // Writes the current tile back and refills its slot with tile k + G + 1.
+  // Writes the current tile back and refills its slot with tile k + nslots
+  // (pipelined launches: the slot's next tile, k + G + 1).
   __device__ __forceinline__ void write_back(const C* init) {
+    uint64_t gthr = 0;
+    uint32_t sthr = 0;
+    thread_offsets(P, tid, P.m - R, gthr, sthr);
+    gthr |= tile_base(P, (uint32_t)((t0 + k) & ((1ll << (P.n - P.m)) - 1)));
     U* gp = reinterpret_cast<U*>(st);
 #pragma unroll
     for (int q = 0; q < NU; ++q) {
@@ -1339,7 +1345,7 @@ struct Pipe {
       }
     }
     group_sync(bar, T);
-    const int64_t kk = k + G + 1;
+    const int64_t kk = k + nslots;
     if (kk < cnt) fetch(kk, init);
   }
 };
@@ -1371,6 +1377,7 @@ struct FwdPass {
   __device__ __forceinline__ bool next() {
     const int r = p.advance();
     if (r == 2) p.build_mats();
+    if (r) p.arrive_wait();
     return r != 0;
   }
 
@@ -1511,6 +1518,7 @@ struct BwdPass {
       }
       p.build_mats();
     }
+    p.arrive_wait();
     return true;
   }
 
@@ -1626,11 +1634,322 @@ struct BwdPass {
   }
 };
 
+// ---------------------------------------------------------------- one tile per CTA
+// The launch variant without the tile pipeline: CTA b owns tile b (tile index
+// = circuit * 2^(n-m) + tile of the circuit), stages it from HBM through
+// registers into shared memory (converting to pair-planar order), builds the
+// pass matrices while its loads are in flight, runs the register phases and
+// writes the tile back.  Passes with many gates run faster this way (their
+// long unrolled phase code is shared by fewer instruction streams per SM).
+// The interface matches FwdPass / BwdPass: next() yields the CTA's one tile.
+
+template <typename real, int R>
+struct FwdTile {
+  using C = cpx<real>;
+  using U = Unit<real>;
+  using S = SUnit<real>;
+  static constexpr int E = UnitsPerAmp<real>::E;
+  static constexpr int NR = 1 << R;
+  static constexpr int NU = NR >> E;
+  const PassParams& P;
+  S* tile;
+  C (*mats)[4];
+  C* st;
+  int tid;
+  uint64_t gthr;
+  uint32_t sthr;
+  uint32_t bu;
+  Regs<real, R> a;
+
+  bool first;
+
+  __device__ __forceinline__ FwdTile(const PassParams& P_, S* tile_, C (*mats_)[4], C* psi, const real* params,
+                                     int n_params, const C* init, int64_t n_tiles, bool norm = true)
+      : P(P_), tile(tile_), mats(mats_), first(true) {
+    (void)n_tiles;
+    tid = threadIdx.x;
+    const int T = blockDim.x;
+    const int64_t circ = (int64_t)(blockIdx.x >> (P.n - P.m));
+    st = psi + (circ << P.n);
+    const real* prm = params ? params + circ * n_params : nullptr;
+    gthr = tile_base(P, blockIdx.x & ((1u << (P.n - P.m)) - 1));
+    sthr = 0;
+    thread_offsets(P, tid, P.m - R, gthr, sthr);
+    U v[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) v[k] = load_unit<real>(P, st, gthr | P.gk[k], init);
+    // matrices while the tile loads are in flight
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
+    if (norm && P.norm_last != kNoNorm) {
+      __syncthreads();
+      norm_scan<real>(P, mats, tid);
+    }
+#pragma unroll
+    for (int k = 0; k < NU; ++k) tile[sthr ^ P.sk[k]] = to_s(v[k]);
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void begin(int f) {
+    const Phase& ph = P.phase[f];
+    bu = 0;
+    for (int b = 0; b < ph.ntid; ++b)
+      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) regs_ld(a, j, tile[bu ^ ph.reg_off[j]]);
+  }
+
+  __device__ __forceinline__ void end(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
+    __syncthreads();
+  }
+
+  // end of a phase whose successor is warp-local (Phase::wlocal)
+  __device__ __forceinline__ void end_w(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) tile[bu ^ ph.reg_off[j]] = regs_st(a, j);
+    __syncwarp();
+  }
+
+  __device__ __forceinline__ void dense(int f) {
+    dense_phase<real>(P, P.phase[f], tile, tid, blockDim.x);
+    __syncthreads();
+  }
+
+
+  // the CTA's one tile
+  __device__ __forceinline__ bool next() {
+    const bool r = first;
+    first = false;
+    return r;
+  }
+  // the tile is staged in pair-planar order: the first and last register
+  // phases need no conversion, nor do dense phases
+  __device__ __forceinline__ void begin_first(int f) { begin(f); }
+  __device__ __forceinline__ void end_last(int f) { end(f); }
+  __device__ __forceinline__ void to_planar() {}
+  __device__ __forceinline__ void to_raw() {}
+  __device__ __forceinline__ void close() {}
+
+  __device__ __forceinline__ void finish() {
+    U* gst = reinterpret_cast<U*>(st);
+#pragma unroll
+    for (int k = 0; k < NU; ++k) gst[(gthr | P.gk[k]) >> E] = from_s(tile[sthr ^ P.sk[k]]);
+  }
+};
+
+// ---------------------------------------------------------------- adjoint pass
+
+template <typename real, int R>
+struct BwdTile {
+  using C = cpx<real>;
+  using U = Unit<real>;
+  using S = SUnit<real>;
+  static constexpr int E = UnitsPerAmp<real>::E;
+  static constexpr int NR = 1 << R;
+  static constexpr int NU = NR >> E;
+  const PassParams& P;
+  S* tp;
+  S* tl;
+  C (*mats)[4];
+  real* gacc;  // per-warp gradient partials (the warp sums, in the state's precision)
+  C* sp;
+  C* sl;
+  double* grad_acc;
+  int64_t circ;
+  int n_params;
+  int tid;
+  uint64_t gthr;
+  uint32_t sthr;
+  uint32_t bu;
+  Regs<real, R> a;
+  Regs<real, R> l;
+
+  bool first;
+
+  __device__ __forceinline__ BwdTile(const PassParams& P_, S* smem, C (*mats_)[4], real* gacc_, C* psi, C* lam,
+                                     const real* params, int n_params_, double* grad_acc_, int64_t n_tiles,
+                                     bool norm = true)
+      : P(P_), mats(mats_), gacc(gacc_), grad_acc(grad_acc_), n_params(n_params_), first(true) {
+    (void)n_tiles;
+    tid = threadIdx.x;
+    const int T = blockDim.x;
+    tp = smem;
+    tl = smem + (1 << (P.m - E));
+    circ = (int64_t)(blockIdx.x >> (P.n - P.m));
+    sp = psi + (circ << P.n);
+    sl = lam + (circ << P.n);
+    const real* prm = params ? params + circ * n_params : nullptr;
+    for (int i = tid; i < P.n_mats; i += T) compute_mat<real>(P, i, prm, mats[i], norm);
+    if (norm && P.norm_last != kNoNorm) {
+      __syncthreads();
+      norm_scan<real>(P, mats, tid);
+    }
+    gthr = tile_base(P, blockIdx.x & ((1u << (P.n - P.m)) - 1));
+    sthr = 0;
+    thread_offsets(P, tid, P.m - R, gthr, sthr);
+    U v[NU], w[NU];
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint64_t g = (gthr | P.gk[k]) >> E;
+      v[k] = reinterpret_cast<const U*>(sp)[g];
+      w[k] = reinterpret_cast<const U*>(sl)[g];
+    }
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      tp[sthr ^ P.sk[k]] = to_s(v[k]);
+      tl[sthr ^ P.sk[k]] = to_s(w[k]);
+    }
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void begin(int f) {
+    const Phase& ph = P.phase[f];
+    bu = 0;
+    for (int b = 0; b < ph.ntid; ++b)
+      if ((tid >> b) & 1) bu ^= ph.tid_off[b];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      regs_ld(a, j, tp[bu ^ ph.reg_off[j]]);
+      regs_ld(l, j, tl[bu ^ ph.reg_off[j]]);
+    }
+  }
+
+  __device__ __forceinline__ void end(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
+      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
+    }
+    __syncthreads();
+  }
+
+  // end of a phase whose successor is warp-local (Phase::wlocal)
+  __device__ __forceinline__ void end_w(int f) {
+    const Phase& ph = P.phase[f];
+#pragma unroll
+    for (int j = 0; j < NU; ++j) {
+      tp[bu ^ ph.reg_off[j]] = regs_st(a, j);
+      tl[bu ^ ph.reg_off[j]] = regs_st(l, j);
+    }
+    __syncwarp();
+  }
+
+  // Warp-reduce one gate's partial gradient into this warp's slot of gate g
+  // (each slot is written by one lane of one warp: no atomics).
+  __device__ __forceinline__ void grad(int g, real part) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((tid & 31) == 0) gacc[(tid >> 5) * kMaxPassGates + g] = part;
+  }
+
+  // Eight gates at once: a transposed butterfly leaves the warp sum of value
+  // j on lanes 4j..4j+3 after 9 shuffles (instead of 8 x 5); gate index < 0
+  // marks an unused value.
+  __device__ __forceinline__ void grad8(real v0, real v1, real v2, real v3, real v4, real v5, real v6, real v7,
+                                        int g0, int g1, int g2, int g3, int g4, int g5, int g6, int g7) {
+    const unsigned lane = tid & 31;
+    real v[8] = {v0, v1, v2, v3, v4, v5, v6, v7};
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const real send = b4 ? v[j] : v[j + 4];
+      const real keep = b4 ? v[j + 4] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const real send = b3 ? v[j] : v[j + 2];
+      const real keep = b3 ? v[j + 2] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    {
+      const real send = b2 ? v[0] : v[1];
+      const real keep = b2 ? v[1] : v[0];
+      v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    if ((lane & 3) == 0) {
+      const int which = (b4 ? 4 : 0) + (b3 ? 2 : 0) + (b2 ? 1 : 0);
+      const int gs[8] = {g0, g1, g2, g3, g4, g5, g6, g7};
+      int g = gs[0];
+#pragma unroll
+      for (int j = 1; j < 8; ++j)
+        if (which == j) g = gs[j];
+      if (g >= 0) gacc[(tid >> 5) * kMaxPassGates + g] = v[0];
+    }
+  }
+
+  __device__ __forceinline__ void dense(int f) {
+    dense_phase<real>(P, P.phase[f], tp, tid, blockDim.x);
+    dense_phase<real>(P, P.phase[f], tl, tid, blockDim.x);
+    __syncthreads();
+  }
+
+
+  // the CTA's one tile
+  __device__ __forceinline__ bool next() {
+    const bool r = first;
+    first = false;
+    return r;
+  }
+  // the tile is staged in pair-planar order: the first and last register
+  // phases need no conversion, nor do dense phases
+  __device__ __forceinline__ void begin_first(int f) { begin(f); }
+  __device__ __forceinline__ void end_last(int f) { end(f); }
+  __device__ __forceinline__ void to_planar() {}
+  __device__ __forceinline__ void to_raw() {}
+  __device__ __forceinline__ void close() {}
+
+  __device__ __forceinline__ void finish() {
+#pragma unroll
+    for (int k = 0; k < NU; ++k) {
+      const uint64_t g = (gthr | P.gk[k]) >> E;
+      reinterpret_cast<U*>(sp)[g] = from_s(tp[sthr ^ P.sk[k]]);
+      reinterpret_cast<U*>(sl)[g] = from_s(tl[sthr ^ P.sk[k]]);
+    }
+    if (P.n_grad) {
+      __syncthreads();
+      const int nw = blockDim.x >> 5;
+      for (int g = tid; g < P.n_gates; g += blockDim.x) {
+        const int32_t slot = P.gate[g].slot;
+        if (slot < 0) continue;
+        double sum = 0.0;
+        for (int w = 0; w < nw; ++w) sum += (double)gacc[w * kMaxPassGates + g];
+        atomicAdd(&grad_acc[circ * n_params + slot], sum * (double)P.gate[g].coef);
+      }
+    }
+  }
+};
+
 }  // namespace dev
 }  // namespace tedq
 
 // Kernel prologues shared by the generic and the generated pass kernels.
 // Generic (interpreted) kernels: plain matrices for the normalised rotations.
+// One tile per CTA (FwdTile / BwdTile): matrices and gradient slots in static
+// shared memory, the tile in dynamic shared memory.
+#define TEDQ_FWD_TILE_PROLOGUE_IMPL(REAL, RB, NORM)                                                     \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                         \
+  tedq::dev::FwdTile<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats,   \
+                                 psi, params, n_params, init, n_tiles, NORM);
+#define TEDQ_BWD_TILE_PROLOGUE_IMPL(REAL, RB, NORM)                                                     \
+  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
+  __shared__ tedq::dev::cpx<REAL> tedq_mats[tedq::kMaxMats][4];                                         \
+  __shared__ REAL tedq_gacc[8 * tedq::kMaxPassGates];                                                   \
+  tedq::dev::BwdTile<REAL, RB> c(P, reinterpret_cast<tedq::dev::SUnit<REAL>*>(tedq_smem_raw), tedq_mats,   \
+                                 tedq_gacc, psi, lam, params, n_params, grad_acc, n_tiles, NORM);
+#define TEDQ_FWD_TILE_PROLOGUE_GENERIC(REAL, RB) TEDQ_FWD_TILE_PROLOGUE_IMPL(REAL, RB, false)
+#define TEDQ_BWD_TILE_PROLOGUE_GENERIC(REAL, RB) TEDQ_BWD_TILE_PROLOGUE_IMPL(REAL, RB, false)
+#define TEDQ_FWD_TILE_PROLOGUE(REAL, RB) TEDQ_FWD_TILE_PROLOGUE_IMPL(REAL, RB, true)
+#define TEDQ_BWD_TILE_PROLOGUE(REAL, RB) TEDQ_BWD_TILE_PROLOGUE_IMPL(REAL, RB, true)
+
+// Tile pipeline (FwdPass / BwdPass): everything in dynamic shared memory.
 #define TEDQ_FWD_PROLOGUE_GENERIC(REAL, RB)                                                             \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
   tedq::dev::FwdPass<REAL, RB> c(P, tedq_smem_raw, psi, params, n_params, init, n_tiles, false);

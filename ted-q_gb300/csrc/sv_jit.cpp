@@ -74,26 +74,33 @@ static void emit_gate(std::ostringstream& o, const PassParams& P, const RGate& r
 static void emit_pass(std::ostringstream& o, const PassParams& P, int index, bool adjoint) {
   const char* real = real_of(P);
   char buf[512];
-  // one CTA of G thread groups and G + 1 tile slots (pipe_layout); as many
-  // CTAs per SM as the shared memory allows
-  const int G = pipe_groups(P, adjoint);
+  // launch bounds: pipelined variant -- one CTA of G thread groups and G + 1
+  // tile slots (pipe_layout); one tile per CTA -- as many CTAs per SM as their
+  // shared memory allows while every thread may keep 128 registers
+  const bool pipe = pass_pipelined(P);
+  PassParams Q = P;
+  Q.pipe = 1;
+  const int G = pipe ? pipe_groups(Q, adjoint) : 1;
   const int threads = G << (P.m - P.R);
-  const int by_smem = (int)(kPipeSmemMax / (pipe_layout(P, G, adjoint).total + 1024));
+  const uint32_t cta_smem = pipe ? pipe_layout(Q, G, adjoint).total
+                                 : tile_dynamic_smem(P, adjoint) + tile_static_smem(P, adjoint);
+  const int by_smem = (int)(kPipeSmemMax / (cta_smem + 1024));
   const int min_blocks = std::max(1, std::min(by_smem, 65536 / (threads * 128)));
+  const char* pro = pipe ? "" : "_TILE";
   if (!adjoint) {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_fwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi,\n"
              "    const %s* __restrict__ params, int n_params, const cpx<%s>* __restrict__ init, long long n_tiles) {\n"
-             "  TEDQ_FWD_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
-             threads, min_blocks, index, real, real, real, real, P.R);
+             "  TEDQ_FWD%s_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
+             threads, min_blocks, index, real, real, real, pro, real, P.R);
   } else {
     snprintf(buf, sizeof buf,
              "extern \"C\" __global__ void __launch_bounds__(%d, %d) tedq_bwd_%d(\n"
              "    const __grid_constant__ tedq::PassParams P, cpx<%s>* __restrict__ psi, cpx<%s>* __restrict__ lam,\n"
              "    const %s* __restrict__ params, int n_params, double* __restrict__ grad_acc, long long n_tiles) {\n"
-             "  TEDQ_BWD_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
-             threads, min_blocks, index, real, real, real, real, P.R);
+             "  TEDQ_BWD%s_PROLOGUE(%s, %d)\n  while (c.next()) {\n",
+             threads, min_blocks, index, real, real, real, pro, real, P.R);
   }
   o << buf;
   int var = 0;
@@ -358,6 +365,7 @@ struct Driver {
   decltype(&cuModuleLoadData) load = nullptr;
   decltype(&cuModuleGetFunction) get = nullptr;
   decltype(&cuFuncSetAttribute) set_attr = nullptr;
+  decltype(&cuFuncGetAttribute) get_attr = nullptr;
   decltype(&cuLaunchKernel) launch = nullptr;
   decltype(&cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
 };
@@ -378,7 +386,8 @@ bool entry(const char* name, F& fn, std::string& why) {
 Driver load_driver() {
   Driver d;
   if (!entry("cuModuleLoadData", d.load, d.why) || !entry("cuModuleGetFunction", d.get, d.why) ||
-      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuLaunchKernel", d.launch, d.why) ||
+      !entry("cuFuncSetAttribute", d.set_attr, d.why) || !entry("cuFuncGetAttribute", d.get_attr, d.why) ||
+      !entry("cuLaunchKernel", d.launch, d.why) ||
       !entry("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy, d.why))
     return d;
   d.ok = true;
@@ -423,44 +432,74 @@ bool jit_load(const std::vector<std::string>& cubins, const std::vector<JitSourc
       err = "missing kernel " + srcs[i].name;
       return false;
     }
-    D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)kPipeSmemMax);
+    // dynamic shared memory up to the per-block limit left by the static part
+    // (the one-tile-per-CTA variant keeps its matrices in static memory)
+    int static_bytes = 0;
+    if (D.get_attr(&static_bytes, CU_FUNC_ATTRIBUTE_SHARED_SIZE_BYTES, f) != CUDA_SUCCESS ||
+        D.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)kPipeSmemMax - static_bytes) !=
+            CUDA_SUCCESS) {
+      err = "cannot set the shared-memory limit of " + srcs[i].name;
+      return false;
+    }
     ((int)i < n_fwd ? out.fwd : out.bwd).push_back(reinterpret_cast<void*>(f));
   }
   return true;
 }
 
-static cudaError_t to_rt(CUresult r) { return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure; }
+// Driver launch results as runtime errors (a refused launch is not reported
+// as a failed kernel).
+static cudaError_t to_rt(CUresult r) {
+  switch (r) {
+    case CUDA_SUCCESS: return cudaSuccess;
+    case CUDA_ERROR_INVALID_VALUE: return cudaErrorInvalidValue;
+    case CUDA_ERROR_OUT_OF_MEMORY: return cudaErrorMemoryAllocation;
+    case CUDA_ERROR_LAUNCH_OUT_OF_RESOURCES: return cudaErrorLaunchOutOfResources;
+    case CUDA_ERROR_INVALID_HANDLE: return cudaErrorInvalidResourceHandle;
+    case CUDA_ERROR_NOT_SUPPORTED: return cudaErrorNotSupported;
+    default: return cudaErrorLaunchFailure;
+  }
+}
 
 static cudaError_t driver_residency(const void* key, int threads, size_t smem, int* per_sm) {
   CUfunction f = reinterpret_cast<CUfunction>(const_cast<void*>(key));
   return driver().occupancy(per_sm, f, threads, smem) == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidConfiguration;
 }
 
-cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P, void* psi, const void* params, int n_params,
+cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P0, void* psi, const void* params, int n_params,
                            const void* init, int64_t batch, cudaStream_t s) {
   (void)dbl;
+  PassParams P = P0;
+  P.pipe = pass_pipelined(P0) ? 1 : 0;
   const int G = pipe_groups(P, false);
-  const unsigned smem = pipe_layout(P, G, false).total, T = (unsigned)G << (P.m - P.R);
+  const unsigned smem = P.pipe ? pipe_layout(P, G, false).total : tile_dynamic_smem(P, false),
+                 T = (unsigned)G << (P.m - P.R);
   long long n_tiles = (long long)(batch << (P.n - P.m));
   CUfunction f = reinterpret_cast<CUfunction>(fn);
-  unsigned grid = 0;
-  cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
-  if (e != cudaSuccess) return e;
+  unsigned grid = (unsigned)n_tiles;
+  if (P.pipe) {
+    cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
+    if (e != cudaSuccess) return e;
+  }
   void* args[] = {const_cast<PassParams*>(&P), &psi, const_cast<void**>(&params), &n_params,
                   const_cast<void**>(&init), &n_tiles};
   return to_rt(driver().launch(f, grid, 1, 1, T, 1, 1, smem, reinterpret_cast<CUstream>(s), args, nullptr));
 }
 
-cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P, void* psi, void* lam, const void* params,
+cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P0, void* psi, void* lam, const void* params,
                            int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
   (void)dbl;
+  PassParams P = P0;
+  P.pipe = pass_pipelined(P0) ? 1 : 0;
   const int G = pipe_groups(P, true);
-  const unsigned smem = pipe_layout(P, G, true).total, T = (unsigned)G << (P.m - P.R);
+  const unsigned smem = P.pipe ? pipe_layout(P, G, true).total : tile_dynamic_smem(P, true),
+                 T = (unsigned)G << (P.m - P.R);
   long long n_tiles = (long long)(batch << (P.n - P.m));
   CUfunction f = reinterpret_cast<CUfunction>(fn);
-  unsigned grid = 0;
-  cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
-  if (e != cudaSuccess) return e;
+  unsigned grid = (unsigned)n_tiles;
+  if (P.pipe) {
+    cudaError_t e = pass_grid_cached(fn, (int)T, smem, n_tiles, driver_residency, grid);
+    if (e != cudaSuccess) return e;
+  }
   void* args[] = {const_cast<PassParams*>(&P), &psi, &lam, const_cast<void**>(&params), &n_params, &grad_acc,
                   &n_tiles};
   return to_rt(driver().launch(f, grid, 1, 1, T, 1, 1, smem, reinterpret_cast<CUstream>(s), args, nullptr));

@@ -6,15 +6,16 @@
 // that loop (``back_prop``, :142-144).
 //
 // Kernels
-//   fwd_pass_kernel  one HBM pass of the forward schedule: persistent CTAs,
-//                    two thread groups each running the pass's register phases
-//                    on one tile (2^m amplitudes, 64 KiB) in shared memory
-//                    while the next tile streams into a third slot; tiles are
-//                    written back in place.
-//   bwd_pass_kernel  one pass of the adjoint sweep over psi and lambda at once
-//                    (same pipeline): for every parameterised gate (in reverse
-//                    order) it adds coef * Im<lambda|G|psi> into the gradient,
-//                    then applies the inverse gate to both states.
+//   fwd_pass_kernel  one HBM pass of the forward schedule, gates dispatched at
+//                    run time (until the circuit's specialised kernels are
+//                    compiled, and for small circuits): a CTA stages one tile
+//                    (2^m amplitudes) in shared memory, runs the pass's
+//                    register phases, writes the tile back in place.
+//   bwd_pass_kernel  one pass of the adjoint sweep over psi and lambda at once:
+//                    for every parameterised gate (in reverse order) it adds
+//                    coef * Im<lambda|G|psi> into the gradient, then applies the
+//                    inverse gate to both states.
+// The specialised kernels (sv_jit.cpp) add the tile pipeline (sv_device.cuh).
 //   expval_kernel    Pauli-string expectations, one read of the state,
 //                    FP32 partial sums per thread/warp and FP64 across warps/CTAs.
 //   probs kernels, lambda_init_kernel, finalize kernels.
@@ -54,11 +55,11 @@ constexpr int kE = dev::UnitsPerAmp<real>::E;
 // Normalised rotations run with their plain matrices here (no pass scale).
 
 template <typename real, int R>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(256, 2)
     fwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi,
                     const real* __restrict__ params, int n_params, const cpx<real>* __restrict__ init,
                     int64_t n_tiles) {
-  TEDQ_FWD_PROLOGUE_GENERIC(real, R)
+  TEDQ_FWD_TILE_PROLOGUE_GENERIC(real, R)
   while (c.next()) {
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];
@@ -85,11 +86,11 @@ __global__ void __launch_bounds__(512, 1)
 }
 
 template <typename real, int R>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(256, 2)
     bwd_pass_kernel(const __grid_constant__ PassParams P, cpx<real>* __restrict__ psi, cpx<real>* __restrict__ lam,
                     const real* __restrict__ params, int n_params, double* __restrict__ grad_acc,
                     int64_t n_tiles) {
-  TEDQ_BWD_PROLOGUE_GENERIC(real, R)
+  TEDQ_BWD_TILE_PROLOGUE_GENERIC(real, R)
   while (c.next()) {
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];
@@ -455,47 +456,30 @@ cudaError_t ensure_smem(K kernel, size_t bytes) {
   return e;
 }
 
-template <typename K>
-cudaError_t runtime_residency(const void* key, int threads, size_t smem, int* per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, reinterpret_cast<K>(const_cast<void*>(key)), threads,
-                                                       smem);
-}
-
+// Generic kernels run one tile per CTA (FwdTile / BwdTile).
 template <typename real, int R>
 cudaError_t fwd_impl(const PassParams& P, void* psi, const void* params, int n_params, const void* init,
                      int64_t batch, cudaStream_t s) {
-  const int G = pipe_groups(P, false);
-  const size_t smem = pipe_layout(P, G, false).total;
-  if (smem > kPipeSmemMax) return cudaErrorInvalidConfiguration;
+  const size_t smem = tile_dynamic_smem(P, false);
   auto kern = fwd_pass_kernel<real, R>;
   cudaError_t e = ensure_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  const int threads = G << (P.m - R);
+  const int threads = 1 << (P.m - R);
   const int64_t n_tiles = batch << (P.n - P.m);
-  unsigned grid = 0;
-  e = pass_grid_cached(reinterpret_cast<const void*>(kern), threads, smem, n_tiles, runtime_residency<decltype(kern)>,
-                       grid);
-  if (e != cudaSuccess) return e;
-  return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
+  return launch_kernel(kern, dim3((unsigned)n_tiles), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
                        static_cast<const real*>(params), n_params, static_cast<const cpx<real>*>(init), n_tiles);
 }
 
 template <typename real, int R>
 cudaError_t bwd_impl(const PassParams& P, void* psi, void* lam, const void* params, int n_params,
                      double* grad_acc, int64_t batch, cudaStream_t s) {
-  const int G = pipe_groups(P, true);
-  const size_t smem = pipe_layout(P, G, true).total;
-  if (smem > kPipeSmemMax) return cudaErrorInvalidConfiguration;
+  const size_t smem = tile_dynamic_smem(P, true);
   auto kern = bwd_pass_kernel<real, R>;
   cudaError_t e = ensure_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  const int threads = G << (P.m - R);
+  const int threads = 1 << (P.m - R);
   const int64_t n_tiles = batch << (P.n - P.m);
-  unsigned grid = 0;
-  e = pass_grid_cached(reinterpret_cast<const void*>(kern), threads, smem, n_tiles, runtime_residency<decltype(kern)>,
-                       grid);
-  if (e != cudaSuccess) return e;
-  return launch_kernel(kern, dim3(grid), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
+  return launch_kernel(kern, dim3((unsigned)n_tiles), dim3(threads), smem, s, P, static_cast<cpx<real>*>(psi),
                        static_cast<cpx<real>*>(lam), static_cast<const real*>(params), n_params, grad_acc, n_tiles);
 }
 

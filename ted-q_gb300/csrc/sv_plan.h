@@ -143,7 +143,8 @@ struct PassParams {
                     // 1 = generate |0..0>, 2 = read the shared initial state
   uint16_t n_gates, n_mats, n_factors, n_grad;
   uint8_t pad_bits;  // init == 2: low idle qubits added by padding
-  uint8_t lam_init;  // adjoint: first pass builds lambda from psi in-kernel
+  uint8_t pipe;      // set per launch: 1 = persistent CTAs with a prefetched tile
+                     // slot per thread group (G + 1 slots), 0 = one tile per CTA
   // normalised rotations: matrix of the last one (kNoNorm = none) and the
   // register phase whose end multiplies the states by the pass's scale
   uint8_t norm_last;
@@ -171,14 +172,16 @@ struct PassParams {
 #endif
 
 // Shared memory of a pass kernel.  A CTA runs G thread groups of 2^(m-R)
-// threads; each group works on one tile at a time and the CTA holds G + 1
-// tile slots, so that while the groups compute, the next tile is already
-// arriving in the spare slot by asynchronous copies.  After the slots: per
-// group the pass matrices and (adjoint) the gradient sums, then one mbarrier
-// per slot.
+// threads; each group works on one tile at a time.  Pipelined (P.pipe = 1):
+// the CTA holds G + 1 tile slots, so that while the groups compute, the next
+// tile is already arriving in the spare slot by asynchronous copies; one tile
+// per CTA (P.pipe = 0): G = 1 and one slot.  After the slots: per group the
+// pass matrices and (adjoint) the gradient sums, then one mbarrier per slot.
 struct PipeLayout {
   uint32_t slot_bytes, mats_off, gacc_off, mbar_off, total;
 };
+
+TEDQ_HD inline int pipe_slots(const PassParams& P, int G) { return P.pipe ? G + 1 : 1; }
 
 constexpr uint32_t kPipeSmemMax = 227u * 1024u;
 
@@ -188,7 +191,7 @@ TEDQ_HD inline PipeLayout pipe_layout(const PassParams& P, int G, bool adjoint) 
   const uint32_t T = 1u << (P.m - P.R);
   const uint32_t W = T >= 32u ? T / 32u : 1u;
   L.slot_bytes = (adjoint ? 2u : 1u) * (amp << P.m);
-  uint32_t off = L.slot_bytes * (uint32_t)(G + 1);
+  uint32_t off = L.slot_bytes * (uint32_t)pipe_slots(P, G);
   L.mats_off = off;
   off += (uint32_t)G * (uint32_t)(P.n_mats > 0 ? P.n_mats : 1) * 4u * amp;
   off = (off + 15u) & ~15u;
@@ -197,16 +200,50 @@ TEDQ_HD inline PipeLayout pipe_layout(const PassParams& P, int G, bool adjoint) 
   if (adjoint) off += (uint32_t)G * (uint32_t)(P.n_gates > 0 ? P.n_gates : 1) * (8u + W * (amp / 2u));
   off = (off + 15u) & ~15u;
   L.mbar_off = off;
-  off += 8u * (uint32_t)(G + 1);
+  off += 8u * (uint32_t)pipe_slots(P, G);
   L.total = off;
   return L;
 }
 
 #if !defined(__CUDACC_RTC__)
-// Two groups (three slots) when they fit in shared memory, else one group
-// with a double-buffered tile; TEDQ_GB300_PIPE_GROUPS=1 asks for one group (a
-// measurement knob).
+// Launch variant of a specialised pass kernel: the tile pipeline (FwdPass /
+// BwdPass) when every circuit has several tiles and the pass is short (at
+// most 64 register gates) or arithmetic-heavy (at least 40 % dense or
+// rotation gates, the kinds with two or more packed FMAs per amplitude);
+// otherwise one tile per CTA (FwdTile / BwdTile).  Measured: the 20-qubit
+// VQC (23-160 gates per pass, half of them rotations) runs faster pipelined
+// in every pass; the 24-qubit MBL chain (60-160 Hadamard, CNOT and phase
+// gates per pass, long code for little arithmetic) and small circuits whose
+// tile is the whole state run faster one tile per CTA.  TEDQ_GB300_PIPE=0 / 1
+// forces a variant (a measurement knob).
+inline bool pass_pipelined(const PassParams& P) {
+  const char* env = getenv("TEDQ_GB300_PIPE");
+  if (env && (env[0] == '0' || env[0] == '1') && !env[1]) return env[0] == '1';
+  if (P.n <= P.m) return false;
+  if (P.n_gates <= 64) return true;
+  int heavy = 0;
+  for (int i = 0; i < P.n_gates; ++i) {
+    const uint8_t k = P.gate[i].kind;
+    heavy += (k == GK_U1 || k == GK_RXT || k == GK_RYT || k == GK_RXN || k == GK_RYN) ? 1 : 0;
+  }
+  return 5 * heavy >= 2 * P.n_gates;
+}
+
+// Shared memory of the one-tile-per-CTA variant: dynamic (the tile) and
+// static (matrices, per-warp gradient slots).
+inline uint32_t tile_dynamic_smem(const PassParams& P, bool adjoint) {
+  return (adjoint ? 32u : 16u) << (P.m - P.e);
+}
+inline uint32_t tile_static_smem(const PassParams& P, bool adjoint) {
+  const uint32_t amp = P.e == 1 ? 8u : 16u;
+  return (uint32_t)kMaxMats * 4u * amp + (adjoint ? 8u * (uint32_t)kMaxPassGates * (amp / 2u) : 0u);
+}
+
+// Pipelined launches: two groups (three slots) when they fit in shared
+// memory, else one group with a double-buffered tile; TEDQ_GB300_PIPE_GROUPS=1
+// asks for one group (a measurement knob).  One tile per CTA: one group.
 inline int pipe_groups(const PassParams& P, bool adjoint) {
+  if (!P.pipe) return 1;
   const uint32_t T = 1u << (P.m - P.R);
   const char* env = getenv("TEDQ_GB300_PIPE_GROUPS");
   const int want = (env && env[0] == '1') ? 1 : 2;
