@@ -77,7 +77,7 @@ static void emit_pass(std::ostringstream& o, const PassParams& P, int index, boo
   // launch bounds: pipelined variant -- one CTA of G thread groups and G + 1
   // tile slots (pipe_layout); one tile per CTA -- as many CTAs per SM as their
   // shared memory allows while every thread may keep 128 registers
-  const bool pipe = pass_pipelined(P);
+  const bool pipe = pass_pipelined(P, adjoint);
   PassParams Q = P;
   Q.pipe = 1;
   const int G = pipe ? pipe_groups(Q, adjoint) : 1;
@@ -469,7 +469,7 @@ cudaError_t jit_launch_fwd(void* fn, bool dbl, const PassParams& P0, void* psi, 
                            const void* init, int64_t batch, cudaStream_t s) {
   (void)dbl;
   PassParams P = P0;
-  P.pipe = pass_pipelined(P0) ? 1 : 0;
+  P.pipe = pass_pipelined(P0, false) ? 1 : 0;
   const int G = pipe_groups(P, false);
   const unsigned smem = P.pipe ? pipe_layout(P, G, false).total : tile_dynamic_smem(P, false),
                  T = (unsigned)G << (P.m - P.R);
@@ -489,7 +489,7 @@ cudaError_t jit_launch_bwd(void* fn, bool dbl, const PassParams& P0, void* psi, 
                            int n_params, double* grad_acc, int64_t batch, cudaStream_t s) {
   (void)dbl;
   PassParams P = P0;
-  P.pipe = pass_pipelined(P0) ? 1 : 0;
+  P.pipe = pass_pipelined(P0, true) ? 1 : 0;
   const int G = pipe_groups(P, true);
   const unsigned smem = P.pipe ? pipe_layout(P, G, true).total : tile_dynamic_smem(P, true),
                  T = (unsigned)G << (P.m - P.R);

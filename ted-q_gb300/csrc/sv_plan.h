@@ -215,11 +215,16 @@ TEDQ_HD inline PipeLayout pipe_layout(const PassParams& P, int G, bool adjoint) 
 // in every pass; the 24-qubit MBL chain (60-160 Hadamard, CNOT and phase
 // gates per pass, long code for little arithmetic) and small circuits whose
 // tile is the whole state run faster one tile per CTA.  TEDQ_GB300_PIPE=0 / 1
-// forces a variant (a measurement knob).
-inline bool pass_pipelined(const PassParams& P) {
+// forces a variant (a measurement knob).  A pass whose two groups and three
+// slots do not fit in shared memory (long complex128 adjoint passes) runs
+// one tile per CTA: one pipelined group per SM would halve the warps.
+inline bool pass_pipelined(const PassParams& P, bool adjoint) {
   const char* env = getenv("TEDQ_GB300_PIPE");
   if (env && (env[0] == '0' || env[0] == '1') && !env[1]) return env[0] == '1';
   if (P.n <= P.m) return false;
+  PassParams Q = P;
+  Q.pipe = 1;
+  if ((2u << (P.m - P.R)) > 1024u || pipe_layout(Q, 2, adjoint).total > kPipeSmemMax) return false;
   if (P.n_gates <= 64) return true;
   int heavy = 0;
   for (int i = 0; i < P.n_gates; ++i) {

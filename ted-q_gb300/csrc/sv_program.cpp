@@ -962,6 +962,15 @@ std::string describe_schedule(const Program& p, bool adjoint) {
     for (int j = 0; j < (1 << (P.R - P.e)); ++j) o << (j ? "," : "") << P.sk[j];
     o << "],\"norm_last\":" << (P.norm_last == kNoNorm ? -1 : (int)P.norm_last)
       << ",\"norm_phase\":" << (P.norm_phase == kNoNorm ? -1 : (int)P.norm_phase);
+    {
+      // launch variant of the specialised kernel and its shared memory per CTA
+      PassParams Q = P;
+      Q.pipe = pass_pipelined(P, adjoint) ? 1 : 0;
+      const int G = pipe_groups(Q, adjoint);
+      const uint32_t smem = Q.pipe ? pipe_layout(Q, G, adjoint).total
+                                   : tile_dynamic_smem(P, adjoint) + tile_static_smem(P, adjoint);
+      o << ",\"pipelined\":" << (int)Q.pipe << ",\"groups\":" << G << ",\"cta_smem\":" << smem;
+    }
     o << ",\"phases\":[";
     for (int f = 0; f < P.n_phases; ++f) {
       const Phase& ph = P.phase[f];

@@ -293,3 +293,92 @@ def test_plan_warp_local_transitions(n, layers, adjoint):
                     assert _warp_units(prev, e, R, w) == _warp_units(ph, e, R, w)
             prev = ph
     assert total == 0 or marked > 0
+
+
+def _vqc20_spec():
+    """The 20-qubit, 10-layer VQC of the benchmark (RX RY RZ per qubit, CNOT ladder)."""
+    rng = np.random.default_rng(0)
+    gates = []
+    for _ in range(10):
+        for q in range(20):
+            for name in ("RX", "RY", "RZ"):
+                gates.append({"name": name, "qubits": [q], "params": [float(rng.uniform(0, 2 * np.pi))],
+                              "trainable": [0]})
+        for q in range(19):
+            gates.append({"name": "CNOT", "qubits": [q, q + 1], "params": [], "trainable": []})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(20)]
+    return {"n": 20, "gates": gates, "meas": meas, "init_state": None}
+
+
+@pytest.mark.parametrize("precision", ["c64", "c128"])
+def test_pass_launch_variants(precision):
+    """Launch variant of every specialised pass (describe's 'pipelined',
+    'groups', 'cta_smem'): the VQC's passes (short or rotation-heavy) are
+    pipelined with two thread groups in complex64; the MBL chain's long passes
+    of Hadamard, CNOT and phase gates run one tile per CTA; a small circuit's
+    whole-state tile runs one tile per CTA; every CTA fits in 227 KB of
+    shared memory."""
+    from tedq_gb300.templates import mbl_spec
+    cases = {"vqc": _vqc20_spec(), "mbl": mbl_spec(24, 3, seed=0), "hea8": _hea_spec(8, 2, seed=1)}
+    for name, spec in cases.items():
+        cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", precision=precision, jit=-1)
+        for adjoint in (False, True):
+            for P in cc.describe(adjoint=adjoint)["passes"]:
+                assert P["cta_smem"] <= 227 * 1024
+                n_gates = sum(len(ph.get("gates", [])) for ph in P["phases"])
+                if name == "hea8":
+                    assert P["pipelined"] == 0
+                if P["pipelined"]:
+                    assert P["groups"] == 2
+                if name == "vqc" and precision == "c64":
+                    assert P["pipelined"] == 1
+                if name == "mbl" and n_gates > 64:
+                    assert P["pipelined"] == 0
+
+
+@pytest.mark.parametrize("G", [1, 2])
+def test_tile_slot_protocol(G):
+    """The pipelined kernel's slot schedule, restated: tile k of a CTA's range
+    belongs to group k % G and lives in slot k % (G + 1); tile j < G + 1 is
+    fetched at start by group (j + G - 1) % G, every later tile k + G + 1 by
+    the group that finished tile k, into the slot it freed.  Under every
+    interleaving of the groups each tile is fetched exactly once, into a free
+    slot, before its group waits for it, and no group waits for a tile that
+    nobody will fetch (no deadlock)."""
+    import random
+    for cnt in range(0, 24):
+        for seed in range(12):
+            rnd = random.Random(seed)
+            fetched, slot_of = set(), {}
+            for j in range(min(G + 1, cnt)):
+                assert (j + G - 1) % G in range(G)
+                fetched.add(j)
+                slot_of[j % (G + 1)] = j
+            k = [g - G for g in range(G)]
+            state = ["next"] * G
+            done, steps = set(), 0
+            while any(st != "exit" for st in state):
+                steps += 1
+                assert steps < 10000, "deadlock"
+                g = rnd.randrange(G)
+                if state[g] == "exit":
+                    continue
+                if state[g] == "next":
+                    nk = k[g] + G
+                    if nk >= cnt:
+                        state[g] = "exit"
+                    elif nk in fetched:
+                        k[g] = nk
+                        state[g] = "work"
+                    continue
+                t = k[g]
+                assert slot_of[t % (G + 1)] == t
+                done.add(t)
+                del slot_of[t % (G + 1)]
+                nxt = t + G + 1
+                if nxt < cnt:
+                    assert nxt not in fetched and (nxt + G - 1) % G == g
+                    fetched.add(nxt)
+                    slot_of[nxt % (G + 1)] = nxt
+                state[g] = "next"
+            assert done == set(range(cnt))
