@@ -558,12 +558,24 @@ class GB300Backend:
         self._init_state = circuit.init_state
         # tn_mode / use_jdopttn / use_cotengra select the tensor-network path
         # (pytorch_backend.py:242-356); the native planner replaces the external
-        # path optimisers, so their objects and hyper_opt are not called
-        # a state measurement's network keeps every output index open
+        # path optimisers, so their objects and hyper_opt are not called.
+        # A state measurement's network keeps every output index open
         # (tensor_network.py:953-955): its value is the state vector
-        # U|0...0>, which the state-vector passes compute directly
-        self._tn = bool(tn_mode or use_jdopttn or use_cotengra) and \
-            not any(_kind(m) == "state" for m in circuit.measurements)
+        # U|0...0>, which the state-vector passes compute directly; so are
+        # outcome probabilities over more qubits than one network per outcome
+        # covers (their outcome axes then still follow the given qubit order,
+        # as the reference's open output indices do)
+        tn_requested = bool(tn_mode or use_jdopttn or use_cotengra)
+        n_q = circuit.num_qubits
+
+        def _wide_probs(m):
+            if _kind(m) != "probs":
+                return False
+            qs = list(range(n_q)) if m.qubits is None else list(dict.fromkeys(int(q) for q in m.qubits))
+            return len(qs) > _Recorded.TN_MAX_PROBS_QUBITS
+
+        self._tn = tn_requested and not any(_kind(m) == "state" or _wide_probs(m) for m in circuit.measurements)
+        self._tn_axes = tn_requested and not self._tn
         if self._tn:
             self._prog = NativeTnPlan(circuit, self._precision, gemm=kwargs.get("tn_gemm", "auto"),
                                       max_rank=kwargs.get("tn_max_rank", 0), repeats=kwargs.get("tn_repeats", 0),
@@ -744,7 +756,13 @@ class GB300Backend:
             elif item[0] == "sample":
                 res.append(self._samples[id(item[1])])
             elif item[0] == "probs":
-                res.append(out[:, item[1]:item[1] + 2 ** item[2]].reshape([B] + [2] * item[2]))
+                p = out[:, item[1]:item[1] + 2 ** item[2]].reshape([B] + [2] * item[2])
+                if self._tn_axes and item[3].qubits is not None:
+                    # tensor-network conventions: outcome axes in the given order
+                    given = list(dict.fromkeys(int(q) for q in item[3].qubits))
+                    srt = sorted(given)
+                    p = p.permute([0] + [1 + srt.index(q) for q in given])
+                res.append(p)
             else:
                 st = psi if prog.pad == 0 else psi[:, :: (1 << prog.pad)]
                 res.append(st.reshape([B] + [2] * prog.n))

@@ -193,3 +193,29 @@ def test_tn_probs_match_state_vector():
     (tn(p1) * w).sum().backward()
     (sv(p2) * w.transpose(-1, -2)).sum().backward()
     torch.testing.assert_close(p1.grad, p2.grad, atol=2e-5, rtol=1e-4)
+
+
+def test_tn_wide_probs_on_state_vector_passes():
+    """probs over more than 8 qubits in the tensor-network mode are evaluated
+    on the state-vector passes (2^9 or more outcome networks would be needed)
+    with the tensor-network mode's outcome axes, in the given qubit order:
+    values against the state-vector mode with its (ascending) axes permuted,
+    and gradients through the permutation."""
+    spec = hea_spec(10, 2)
+    given = [9, 0, 4, 1, 8, 2, 7, 3, 6]
+    spec["meas"] = [{"kind": "probs", "qubits": given}]
+    tn = _tn(spec, "c64", "fp32")
+    assert not tn._tn
+    sv = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300")
+    n = len(flat_params(spec))
+    gen = torch.Generator().manual_seed(11)
+    P = (torch.rand(2, n, generator=gen) * 6.28).to(DEV)
+    axes = [sorted(given).index(q) for q in given]
+    want = sv.execute_batch(P)[:, 0].permute([0] + [1 + a for a in axes])
+    torch.testing.assert_close(tn.execute_batch(P)[:, 0], want, atol=1e-6, rtol=1e-5)
+    w = torch.rand([2] * 9, generator=gen).to(DEV)
+    p1 = P[0].clone().requires_grad_(True)
+    p2 = P[0].clone().requires_grad_(True)
+    (tn(p1)[0] * w).sum().backward()
+    (sv(p2)[0].permute(axes) * w).sum().backward()
+    torch.testing.assert_close(p1.grad, p2.grad, atol=1e-5, rtol=1e-4)

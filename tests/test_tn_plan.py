@@ -196,15 +196,23 @@ def test_tn_capi_rejects_probs_and_bad_input():
 def test_tn_mode_state_and_wide_probs():
     """A state measurement's network keeps every output index open
     (tensor_network.py:953-955): the tensor-network mode evaluates it on the
-    state-vector passes; probs over more than 8 qubits are rejected."""
+    state-vector passes, and so are probs over more than 8 qubits (2^9 or
+    more outcome networks), whose outcome axes keep the tensor-network
+    convention (given qubit order)."""
     spec = random_spec(1)
     spec["meas"] = [{"kind": "state"}]
     cc = plan(spec)
-    assert not cc._tn and cc._prog.has_state
+    assert not cc._tn and cc._prog.has_state and cc._tn_axes
     spec = random_spec(2, n=10)
     spec["meas"] = [{"kind": "probs", "qubits": None}]  # 2^10 outcome networks
-    with pytest.raises(NotImplementedError):
-        plan(spec)
+    cc = plan(spec)
+    assert not cc._tn and cc._tn_axes
+    spec["meas"] = [{"kind": "probs", "qubits": [9, 0, 4, 1, 8, 2, 7, 3, 6]}]
+    cc = plan(spec)
+    assert not cc._tn and cc._tn_axes
+    spec["meas"] = [{"kind": "probs", "qubits": [9, 0, 4]}]  # 8 networks: tensor-network mode
+    cc = plan(spec)
+    assert cc._tn and not cc._tn_axes
 
 
 @pytest.mark.parametrize("seed", range(6))
