@@ -351,21 +351,25 @@ int32_t run_forward(tedq_program_t* prog, const void* params, int64_t batch, voi
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/init");
   }
   JitKernels* jk = p.fwd.passes.empty() ? nullptr : forward_only ? jit_kernels_if_loaded(prog) : jit_kernels(prog);
+  // From |0...0> the passes skip all-zero tiles (PassParams::zero_outer): the
+  // state is cleared first so that the skipped amplitudes read as zero.  A
+  // given initial state has no zero tiles to count on.
+  if (!init && !p.fwd.passes.empty() && p.fwd.passes[0].zero_outer) {
+    e = cudaMemsetAsync(psi, 0, (size_t)(batch << p.ns) * (dbl ? 16 : 8), s);
+    if (e != cudaSuccess) return cuda_fail(e, "tedq_run/memset");
+  }
   for (size_t i = 0; i < p.fwd.passes.size(); ++i) {
+    PassParams P = p.fwd.passes[i];
+    if (init) P.zero_outer = 0;
     if (i == 0) {
-      PassParams P = p.fwd.passes[0];
       P.init = init ? 2 : 1;
       P.pad_bits = (uint8_t)p.pad;
-      e = timed(prog, 0, batch << p.ns, s, [&] {
-        return jk ? jit_launch_fwd(jk->fwd[0], dbl, P, psi, params, p.n_params, init, batch, s)
-                  : launch_fwd_pass(dbl, P, psi, params, p.n_params, init, batch, s);
-      });
-    } else {
-      e = timed(prog, 0, batch << p.ns, s, [&] {
-        return jk ? jit_launch_fwd(jk->fwd[i], dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s)
-                  : launch_fwd_pass(dbl, p.fwd.passes[i], psi, params, p.n_params, nullptr, batch, s);
-      });
     }
+    const void* ini = i == 0 ? init : nullptr;
+    e = timed(prog, 0, batch << p.ns, s, [&] {
+      return jk ? jit_launch_fwd(jk->fwd[i], dbl, P, psi, params, p.n_params, ini, batch, s)
+                : launch_fwd_pass(dbl, P, psi, params, p.n_params, ini, batch, s);
+    });
     if (e != cudaSuccess) return cuda_fail(e, "tedq_run/pass");
   }
   char* ws = static_cast<char*>(workspace);

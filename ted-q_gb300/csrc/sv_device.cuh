@@ -1258,10 +1258,15 @@ struct Pipe {
     const uint32_t tic = (uint32_t)(gt & ((1ll << (P.n - P.m)) - 1));
     // staging offsets are recomputed per tile (not kept in registers across
     // the register phases)
+    const uint64_t tb = tile_base(P, tic);
+    if (tb & P.zero_outer) {  // all-zero tile: nothing to copy
+      mbar_arrive(&mbar[s]);
+      return;
+    }
     uint64_t gth = 0;
     uint32_t sthr = 0;
     thread_offsets(P, tid, P.m - R, gth, sthr);
-    const uint64_t gb = tile_base(P, tic) | gth;
+    const uint64_t gb = tb | gth;
     const C* src = psi + (c << P.n);
     if (ADJ || P.init == 0) {
 #pragma unroll
@@ -1295,6 +1300,20 @@ struct Pipe {
     st = psi + (c << P.n);
     if (ADJ) sl = lam + (c << P.n);
     return 2;
+  }
+
+  // The current tile is all zero (forward sweep from |0...0>, qubits not yet
+  // touched): it stays zero and is neither computed nor written.
+  __device__ __forceinline__ bool zero_tile() const {
+    return (tile_base(P, (uint32_t)((t0 + k) & ((1ll << (P.n - P.m)) - 1))) & P.zero_outer) != 0;
+  }
+
+  // Releases a zero tile's slot: its (copy-free) phase must complete before
+  // the slot is refilled.
+  __device__ __forceinline__ void skip(const C* init) {
+    arrive_wait();
+    const int64_t kk = k + nslots;
+    if (kk < cnt) fetch(kk, init);
   }
 
   // Waits for the current tile's copies.
@@ -1362,23 +1381,34 @@ struct FwdPass {
   Pipe<real, R, false> p;
   const C* init;
   C (*mats)[4];
+  int64_t mats_circ;  // circuit whose matrices are built (-1: none)
   uint32_t bu;
   Regs<real, R> a;
 
   __device__ __forceinline__ FwdPass(const PassParams& P_, unsigned char* smem, C* psi, const real* params,
                                      int n_params, const C* init_, int64_t n_tiles, bool norm = true)
-      : p(P_, smem, psi, nullptr, params, n_params, n_tiles, norm), init(init_) {
+      : p(P_, smem, psi, nullptr, params, n_params, n_tiles, norm), init(init_), mats_circ(-1) {
     mats = p.mats;
     __syncthreads();
     p.start(init);
   }
 
-  // next tile of this thread's group (false: none left)
+  // next tile of this thread's group (false: none left); all-zero tiles are
+  // skipped, the matrices built for the circuit of the first one computed
   __device__ __forceinline__ bool next() {
-    const int r = p.advance();
-    if (r == 2) p.build_mats();
-    if (r) p.arrive_wait();
-    return r != 0;
+    for (;;) {
+      if (!p.advance()) return false;
+      if (p.P.zero_outer && p.zero_tile()) {
+        p.skip(init);
+        continue;
+      }
+      if (p.circ != mats_circ) {
+        p.build_mats();
+        mats_circ = p.circ;
+      }
+      p.arrive_wait();
+      return true;
+    }
   }
 
   // Register phases read the tile in pair-planar order, except the first,
@@ -1673,6 +1703,12 @@ struct FwdTile {
     st = psi + (circ << P.n);
     const real* prm = params ? params + circ * n_params : nullptr;
     gthr = tile_base(P, blockIdx.x & ((1u << (P.n - P.m)) - 1));
+    // an all-zero tile (untouched qubits set, forward sweep from |0...0>)
+    // stays zero: nothing to read, compute or write
+    if (gthr & P.zero_outer) {
+      first = false;
+      return;
+    }
     sthr = 0;
     thread_offsets(P, tid, P.m - R, gthr, sthr);
     U v[NU];

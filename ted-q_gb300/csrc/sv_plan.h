@@ -150,6 +150,12 @@ struct PassParams {
   uint8_t norm_last;
   uint8_t norm_phase;
   uint8_t hi[kMaxTileBits];      // global bit of tile bit c+i
+  // Forward sweeps from |0...0>: qubits that no earlier pass has touched are
+  // still |0>, so a tile whose base has any of these (outer) bits set is all
+  // zero before and after the pass and is skipped (not read, computed or
+  // written; the caller clears the state before the first pass).  0 for the
+  // adjoint sweep and for a user-given initial state.
+  uint64_t zero_outer;
   uint8_t outer[kMaxStateBits];  // global bit of outer-index bit i
   // Tile staging: thread tid stages units u = tid + k * 2^(m-R), k < 2^(R-e).
   // Global amplitude offset = tile base | OR of gtid[b] over set bits b of

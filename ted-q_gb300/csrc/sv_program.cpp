@@ -930,6 +930,21 @@ Program* compile_program(const tedq_gate_t* gates, int n_gates, int n_qubits, co
   if (p->fuse)
     p->fused = fuse_one_qubit_runs(p->elem, p->ns, p->phase_free && norm_f && norm_u && jit_expected);
   p->fwd = schedule(p->fused, p->ns, gf, false, p->fuse != 0, p->phase_free, norm_f);
+  // zero tiles of the forward sweep from |0...0>: outer bits of a pass that
+  // no earlier pass had among its tile bits (TEDQ_GB300_ZERO_TILES=0 turns
+  // the skipping off, a measurement knob)
+  {
+    const char* zt = getenv("TEDQ_GB300_ZERO_TILES");
+    const bool skip = !(zt && zt[0] == '0');
+    uint64_t touched = 0;
+    for (PassParams& P : p->fwd.passes) {
+      uint64_t tile = (1ull << P.c) - 1, outer = 0;
+      for (int j = 0; j < P.m - P.c; ++j) tile |= 1ull << P.hi[j];
+      for (int j = 0; j < P.n_outer; ++j) outer |= 1ull << P.outer[j];
+      P.zero_outer = skip ? (outer & ~touched) : 0;
+      touched |= tile;
+    }
+  }
   std::vector<HGate> rev(p->elem.rbegin(), p->elem.rend());
   p->bwd = schedule(rev, p->ns, gb, true, p->fuse != 0, true, norm_b);
   compile_measurements(*p, meas, n_meas);
@@ -969,7 +984,8 @@ std::string describe_schedule(const Program& p, bool adjoint) {
       const int G = pipe_groups(Q, adjoint);
       const uint32_t smem = Q.pipe ? pipe_layout(Q, G, adjoint).total
                                    : tile_dynamic_smem(P, adjoint) + tile_static_smem(P, adjoint);
-      o << ",\"pipelined\":" << (int)Q.pipe << ",\"groups\":" << G << ",\"cta_smem\":" << smem;
+      o << ",\"pipelined\":" << (int)Q.pipe << ",\"groups\":" << G << ",\"cta_smem\":" << smem
+        << ",\"zero_outer\":" << P.zero_outer;
     }
     o << ",\"phases\":[";
     for (int f = 0; f < P.n_phases; ++f) {

@@ -183,6 +183,43 @@ def test_gradients_alone_equal_in_batch(precision, jit):
         torch.testing.assert_close(pa.grad[0], pb.grad[b], **tol)
 
 
+@pytest.mark.parametrize("jit,pipe", [(-1, "0"), (1, "0"), (1, "1")],
+                         ids=["generic", "specialised-one-tile", "specialised-pipelined"])
+def test_zero_tile_skipping_is_exact(monkeypatch, jit, pipe):
+    """Forward sweeps from |0...0> skip the tiles whose untouched qubits are
+    set (all zero before and after the pass) after clearing the state: values,
+    final states and adjoint gradients equal those of the same program planned
+    without skipping (TEDQ_GB300_ZERO_TILES=0), in every kernel variant; a
+    given initial state disables the skipping."""
+    monkeypatch.setenv("TEDQ_GB300_PIPE", pipe)
+    spec = _vqc_spec(16, 3, seed=4)
+    circ = qai.Circuit.from_spec(spec)
+    skip = circ.compilecircuit(backend="gb300", jit=jit)
+    assert skip.describe()["passes"][0]["zero_outer"] != 0
+    monkeypatch.setenv("TEDQ_GB300_ZERO_TILES", "0")
+    full = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=jit)
+    assert all(P["zero_outer"] == 0 for P in full.describe()["passes"])
+    for cc in (skip, full):
+        if jit == 1:
+            assert cc._prog.jit_wait() is None
+    gen = torch.Generator().manual_seed(4)
+    params = (torch.rand(5, skip.num_params, generator=gen) * 2 * np.pi).to(DEV)
+    outs, grads, states = [], [], []
+    for cc in (skip, full):
+        pd = params.clone().requires_grad_(True)
+        out = cc.execute_batch(pd)
+        out.sum().backward()
+        outs.append(out.detach())
+        grads.append(pd.grad)
+        out_f, psi = cc._forward(params)
+        states.append(psi.clone())
+    # (expectation values and gradients are summed with FP64 atomics: equal
+    # up to the order of those additions)
+    torch.testing.assert_close(outs[0], outs[1], atol=1e-7, rtol=0)
+    torch.testing.assert_close(grads[0], grads[1], atol=1e-6, rtol=1e-6)
+    torch.testing.assert_close(states[0], states[1], atol=0, rtol=0)
+
+
 def test_unfused_equals_fused():
     spec = _vqc_spec(11, 2, seed=5)
     a = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)

@@ -382,3 +382,20 @@ def test_tile_slot_protocol(G):
                     slot_of[nxt % (G + 1)] = nxt
                 state[g] = "next"
             assert done == set(range(cnt))
+
+
+def test_zero_tile_masks():
+    """Forward sweeps from |0...0> skip all-zero tiles: a pass's zero_outer
+    mask holds exactly its outer bits that no earlier forward pass had among
+    its tile bits (the first pass: all its outer bits); adjoint passes have
+    none."""
+    spec = _vqc20_spec()
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=-1)
+    touched = 0
+    for P in cc.describe()["passes"]:
+        tile = ((1 << P["c"]) - 1) | sum(1 << b for b in P["hi"])
+        outer = sum(1 << b for b in P["outer"])
+        assert P["zero_outer"] == outer & ~touched
+        touched |= tile
+    assert cc.describe()["passes"][0]["zero_outer"] == sum(1 << b for b in cc.describe()["passes"][0]["outer"])
+    assert all(P["zero_outer"] == 0 for P in cc.describe(adjoint=True)["passes"])
