@@ -103,3 +103,30 @@ def test_specialised_kernels_compile_for_sm103a(tmp_path, monkeypatch):
         cc = qai.Circuit.from_spec(case).compilecircuit(backend="gb300", precision=precision, jit=1)
         assert cc._prog.jit_wait() is None
     assert any(p.suffix == ".cubin" for p in tmp_path.iterdir())
+
+
+@pytest.mark.parametrize("pipe", ["0", "1"])
+def test_specialised_kernel_variants_compile(tmp_path, monkeypatch, pipe):
+    """Both launch variants of the specialised kernels (tile pipeline and one
+    tile per CTA) compile with NVRTC for sm_103a, in both precisions, for a
+    circuit of several tiles per state that contains every gate kind
+    (including dense phases at the start and end of passes)."""
+    monkeypatch.setenv("TEDQ_GB300_CACHE", str(tmp_path))
+    monkeypatch.setenv("TEDQ_GB300_PIPE", pipe)
+    from conftest import load_cases
+    case = dict(next(c for c in load_cases() if c["name"] == "all_gates_n5"))
+    n = 15
+    gates = list(case["gates"])
+    for q in range(5, n):
+        gates.append({"name": "RY", "qubits": [q], "params": [0.1 * q], "trainable": [0]})
+        gates.append({"name": "CNOT", "qubits": [q - 1, q], "params": [], "trainable": []})
+    gates += list(case["gates"])
+    case.update(n=n, gates=gates)
+    for precision in ("c64", "c128"):
+        cc = qai.Circuit.from_spec(case).compilecircuit(backend="gb300", precision=precision, jit=1)
+        for adjoint in (False, True):
+            passes = cc.describe(adjoint=adjoint)["passes"]
+            assert any(P["outer"] for P in passes)
+            assert all(P["pipelined"] == int(pipe) for P in passes if P["outer"])
+        assert cc._prog.jit_wait() is None
+    assert any(p.suffix == ".cubin" for p in tmp_path.iterdir())

@@ -220,6 +220,50 @@ def test_zero_tile_skipping_is_exact(monkeypatch, jit, pipe):
     torch.testing.assert_close(states[0], states[1], atol=0, rtol=0)
 
 
+def _unitary(k, rng):
+    a = rng.normal(size=(2 ** k, 2 ** k)) + 1j * rng.normal(size=(2 ** k, 2 ** k))
+    q, r = np.linalg.qr(a)
+    u = q * (np.diag(r) / np.abs(np.diag(r)))
+    return [[float(v.real), float(v.imag)] for v in u.reshape(-1)]
+
+
+@pytest.mark.parametrize("jit,pipe", [(-1, "0"), (1, "0"), (1, "1")],
+                         ids=["generic", "specialised-one-tile", "specialised-pipelined"])
+def test_dense_phases_across_tiles(monkeypatch, jit, pipe):
+    """Generic 2- and 3-qubit unitaries become dense shared-memory phases;
+    placed first and last in the circuit (and between rotations) they open
+    and close passes, where the pipelined kernels convert the tile between
+    HBM order and pair-planar order.  15 qubits (several tiles per state),
+    complex64 values and adjoint gradients against the complex128 oracle."""
+    monkeypatch.setenv("TEDQ_GB300_PIPE", pipe)
+    rng = np.random.default_rng(31)
+    n = 15
+    gates = [{"name": "Unitary", "qubits": [0, 1, 2], "params": [], "trainable": [], "matrix": _unitary(3, rng)}]
+    for q in range(n):
+        gates.append({"name": "RY", "qubits": [q], "params": [float(rng.uniform(0, 6.28))], "trainable": [0]})
+    gates.append({"name": "Unitary", "qubits": [13, 6], "params": [], "trainable": [], "matrix": _unitary(2, rng)})
+    for q in range(n - 1):
+        gates.append({"name": "CNOT", "qubits": [q, q + 1], "params": [], "trainable": []})
+        gates.append({"name": "RX", "qubits": [q], "params": [float(rng.uniform(0, 6.28))], "trainable": [0]})
+    gates.append({"name": "Unitary", "qubits": [14, 7, 1], "params": [], "trainable": [], "matrix": _unitary(3, rng)})
+    meas = [{"kind": "expval", "list": False, "obs": [{"name": "PauliZ", "qubits": [q]}]} for q in range(0, n, 2)]
+    spec = {"n": n, "gates": gates, "meas": meas, "init_state": None}
+    cc = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", jit=jit)
+    if jit == 1:
+        assert cc._prog.jit_wait() is None
+    dense = [ph["type"] for P in cc.describe()["passes"] + cc.describe(adjoint=True)["passes"] for ph in P["phases"]]
+    assert 1 in dense
+    gen = torch.Generator().manual_seed(31)
+    params = torch.rand(3, cc.num_params, generator=gen, dtype=torch.float64) * 2 * np.pi
+    pd = params.to(DEV, torch.float32).requires_grad_(True)
+    out = cc.execute_batch(pd)
+    out.sum().backward()
+    for b in range(3):
+        want, want_g = oracle.value_and_grad(spec, params[b], np.ones(out.shape[1]), torch.complex128)
+        np.testing.assert_allclose(out[b].detach().cpu().double().numpy(), want.numpy(), atol=1e-5)
+        np.testing.assert_allclose(pd.grad[b].cpu().double().numpy(), want_g.numpy(), atol=5e-5, rtol=1e-4)
+
+
 def test_unfused_equals_fused():
     spec = _vqc_spec(11, 2, seed=5)
     a = qai.Circuit.from_spec(spec).compilecircuit(backend="gb300", requires_grad=False)
