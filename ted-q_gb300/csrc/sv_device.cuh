@@ -1117,18 +1117,21 @@ __device__ __forceinline__ void thread_offsets(const PassParams& P, int tid, int
 }
 
 // ---------------------------------------------------------------- tile pipeline
-// A pass kernel is persistent: CTA b takes a contiguous range of the launch's
-// tiles (tile index = circuit * 2^(n-m) + tile of the circuit) and runs it in
-// G thread groups that take the range's tiles in turn (group k % G takes tile
-// k).  Tile k lives in slot k % (G + 1).  When a group has written tile k
-// back to HBM it issues the asynchronous copies (cp.async, 16 bytes a thread)
-// of tile k + G + 1 into the slot it just freed, so HBM reads run while the
-// groups compute; the copies arrive on the slot's mbarrier, which the group
-// owning the tile waits on.  Groups synchronise with their own named barrier
-// and never wait on each other except through the slot mbarriers, so one
-// group's shared-memory transitions overlap the other's arithmetic.  The
-// matrices are built once per circuit and group, adjoint gradients are summed
-// per warp in FP64 over all tiles of a circuit and added to HBM once.
+// The pipelined variant of a specialised pass kernel is persistent: CTA b
+// takes a contiguous range of the launch's tiles (tile index = circuit *
+// 2^(n-m) + tile of the circuit) and runs it in G thread groups that take the
+// range's tiles in turn (group k % G takes tile k).  Tile k lives in slot
+// k % (G + 1).  When a group has written tile k back to HBM it issues the
+// asynchronous copies (cp.async, 16 bytes a thread) of tile k + G + 1 into the
+// slot it just freed, so HBM reads run while the groups compute; the copies
+// arrive on the slot's mbarrier, which the group owning the tile waits on.
+// Groups synchronise with their own named barrier and never wait on each
+// other except through the slot mbarriers, so one group's shared-memory
+// transitions overlap the other's arithmetic.  The matrices are built once
+// per circuit and group; adjoint gradient partials are summed per warp in
+// FP32 over at most 8 tiles, folded into per-gate FP64 sums and added to HBM
+// once per circuit and group.  All-zero tiles of a forward sweep from
+// |0...0> (PassParams::zero_outer) are skipped.
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -1985,14 +1988,8 @@ struct BwdTile {
 #define TEDQ_FWD_TILE_PROLOGUE(REAL, RB) TEDQ_FWD_TILE_PROLOGUE_IMPL(REAL, RB, true)
 #define TEDQ_BWD_TILE_PROLOGUE(REAL, RB) TEDQ_BWD_TILE_PROLOGUE_IMPL(REAL, RB, true)
 
-// Tile pipeline (FwdPass / BwdPass): everything in dynamic shared memory.
-#define TEDQ_FWD_PROLOGUE_GENERIC(REAL, RB)                                                             \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
-  tedq::dev::FwdPass<REAL, RB> c(P, tedq_smem_raw, psi, params, n_params, init, n_tiles, false);
-#define TEDQ_BWD_PROLOGUE_GENERIC(REAL, RB)                                                             \
-  extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
-  tedq::dev::BwdPass<REAL, RB> c(P, tedq_smem_raw, psi, lam, params, n_params, grad_acc, n_tiles, false);
-
+// Tile pipeline (FwdPass / BwdPass, specialised kernels only): everything in
+// dynamic shared memory.
 #define TEDQ_FWD_PROLOGUE(REAL, RB)                                                                     \
   extern __shared__ __align__(16) unsigned char tedq_smem_raw[];                                        \
   tedq::dev::FwdPass<REAL, RB> c(P, tedq_smem_raw, psi, params, n_params, init, n_tiles);
