@@ -182,8 +182,13 @@ def run_pass(P, psi, prm, lam=None, grads=None):
     n_outer = len(P["outer"])
     T = 1 << (m - R)
     phys = np.array([(swz_unit(t >> e) << e) | (t & ((1 << e) - 1)) for t in range(1 << m)])
+    zero_outer = P.get("zero_outer", 0)
     for tile in range(1 << n_outer):
         g = _tile_index(P, tile)
+        if zero_outer and (int(g[0]) & zero_outer):
+            # the device skips this tile: it must be (and stays) all zero
+            assert not np.any(psi[g]), "a tile the kernels skip holds non-zero amplitudes"
+            continue
         tp = np.zeros(1 << m, dtype=complex)
         tp[phys] = psi[g]
         tl = None
@@ -239,6 +244,9 @@ def pauli_apply(psi, x, z):
 
 
 def forward(desc, prm, init=None):
+    """From |0...0> the passes skip the tiles their zero_outer masks name (as
+    the kernels do, after clearing the state); a given initial state runs
+    every tile (the launcher clears the masks)."""
     ns = desc["state_qubits"]
     psi = np.zeros(1 << ns, dtype=complex)
     if init is None:
@@ -247,7 +255,7 @@ def forward(desc, prm, init=None):
         pad = ns - desc["n"]
         psi[::1 << pad] = init
     for P in desc["passes"]:
-        run_pass(P, psi, prm)
+        run_pass(P if init is None else dict(P, zero_outer=0), psi, prm)
     return psi
 
 
